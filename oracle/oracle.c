@@ -1,0 +1,365 @@
+/* Oracle (test infrastructure only): CPU restatement of Mini-FEM's assembly step
+ * (element integration, CSR scatter-add, block-Jacobi preconditioner), written
+ * from the reference's algorithm.  It is the checker for the CUDA path and the
+ * timed CPU baseline ("port") of the benchmark; nothing in the product links it.
+ *
+ * Parity pins: this restatement is compared bit for bit with the reference's own
+ * sources compiled here (oracle/Makefile -> oracle/_ref) on the committed golden
+ * meshes; the 3x3 inverse (lapack3.h) is compared with scipy's LAPACK.
+ *
+ * Compile with -O2 -ffp-contract=off so that no product/sum pair is fused: the
+ * expression trees below are the reference's, operation for operation.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#include "oracle.h"
+#include "lapack3.h"
+
+#define DIM_ELEM 4
+#define DIM_NODE 3
+
+/* Coefficient form.  The reference operator has fixed constants
+ * (assembly.cc:423-446: 2.25 and 1.25 for ela, 1 for lap).  The extended form
+ * weights the Laplacian by kappa and the elasticity blocks by the Lame
+ * combinations A = lambda + 2 mu, B = lambda + mu and mu:
+ *     diag  c(a,a) = ((p_aa*A' + p_bb*B') + p_cc*C')   positional order kept
+ *     off   c(a,b) = p_ab * B
+ * which reproduces the reference bit for bit at A = 2.25, B = 1.25, mu = 1
+ * (lambda = 0.25, mu = 1), since p*1.0 == p exactly. */
+typedef struct { double A, B, mu, kappa; } orc_coef_t;
+
+static inline orc_coef_t orc_coef(const double *coef, int operatorID, long e)
+{
+    orc_coef_t c = {2.25, 1.25, 1.0, 1.0};
+    if (!coef) return c;
+    if (operatorID == 0) {
+        c.kappa = coef[e];
+    } else {
+        double E = coef[2 * e], nu = coef[2 * e + 1];
+        double lam = (E * nu) / ((1.0 + nu) * (1.0 - 2.0 * nu));
+        double mu = E / (2.0 * (1.0 + nu));
+        c.A = lam + 2.0 * mu;
+        c.B = lam + mu;
+        c.mu = mu;
+    }
+    return c;
+}
+
+/* src/assembly.cc:85-121 elem_coef_seq. */
+static inline void orc_elem_coef(double g[DIM_ELEM][DIM_NODE], const double *coord,
+                                 const int *elemToNode, long elem)
+{
+    double xa, xb, xc, ya, yb, yc, za, zb, zc, vol;
+    for (int i = 0; i < DIM_ELEM; i++) {
+        long node = elemToNode[elem * DIM_ELEM + i] - 1;
+        for (int j = 0; j < DIM_NODE; j++) g[i][j] = coord[node * DIM_NODE + j];
+    }
+    xa = g[0][0] - g[3][0];
+    xb = g[2][0] - g[3][0];
+    xc = g[1][0] - g[3][0];
+    ya = g[0][1] - g[3][1];
+    yb = g[2][1] - g[3][1];
+    yc = g[1][1] - g[3][1];
+    za = g[0][2] - g[3][2];
+    zb = g[2][2] - g[3][2];
+    zc = g[1][2] - g[3][2];
+    g[0][0] = yb * zc - yc * zb;
+    g[0][1] = zb * xc - zc * xb;
+    g[0][2] = xb * yc - xc * yb;
+    g[1][0] = ya * zb - yb * za;
+    g[1][1] = za * xb - zb * xa;
+    g[1][2] = xa * yb - xb * ya;
+    g[2][0] = yc * za - ya * zc;
+    g[2][1] = zc * xa - za * xc;
+    g[2][2] = xc * ya - xa * yc;
+    g[3][0] = -(g[0][0] + g[1][0] + g[2][0]);
+    g[3][1] = -(g[0][1] + g[1][1] + g[2][1]);
+    g[3][2] = -(g[0][2] + g[1][2] + g[2][2]);
+    vol = xa * g[0][0] + ya * g[0][1] + za * g[0][2];
+    double r = 1. / vol;
+    for (int i = 0; i < DIM_ELEM; i++)
+        for (int j = 0; j < DIM_NODE; j++) g[i][j] *= r;
+}
+
+/* One (j,k) contribution added into v: assembly.cc:423-446 (ela) and
+ * assembly.cc:555-557 (lap). */
+static inline void orc_add_block(double *v, const double *gj, const double *gk,
+                                 int operatorID, const orc_coef_t *c)
+{
+    if (operatorID == 0) {
+        double s = gj[0] * gk[0] + gj[1] * gk[1] + gj[2] * gk[2];
+        v[0] += c->kappa * s;
+    } else {
+        v[0] += gj[0] * gk[0] * c->A + gj[1] * gk[1] * c->mu + gj[2] * gk[2] * c->mu;
+        v[1] += gj[0] * gk[1] * c->B;
+        v[2] += gj[0] * gk[2] * c->B;
+        v[3] += gj[1] * gk[0] * c->B;
+        v[4] += gj[0] * gk[0] * c->mu + gj[1] * gk[1] * c->A + gj[2] * gk[2] * c->mu;
+        v[5] += gj[1] * gk[2] * c->B;
+        v[6] += gj[2] * gk[0] * c->B;
+        v[7] += gj[2] * gk[1] * c->B;
+        v[8] += gj[0] * gk[0] * c->mu + gj[1] * gk[1] * c->mu + gj[2] * gk[2] * c->A;
+    }
+}
+
+void orc_node_to_elem(int nbNodes, int nbElem, const int *elemToNode, int *index,
+                      int *value)
+{
+    int *fill = (int *)calloc((size_t)nbNodes + 1, sizeof(int));
+    memset(index, 0, sizeof(int) * ((size_t)nbNodes + 1));
+    for (long i = 0; i < (long)nbElem * DIM_ELEM; i++) index[elemToNode[i]]++;
+    for (int i = 0; i < nbNodes; i++) index[i + 1] += index[i];
+    for (long e = 0; e < nbElem; e++)
+        for (int k = 0; k < DIM_ELEM; k++) {
+            int n = elemToNode[e * DIM_ELEM + k] - 1;
+            value[index[n] + fill[n]++] = (int)e;
+        }
+    free(fill);
+}
+
+void orc_create_nodeToNode(int *row, int *col, const int *nteIndex,
+                           const int *nteValue, const int *elemToNode, int nbNodes)
+{
+    int ctr = 0;
+    for (int i = 0; i < nbNodes; i++) {
+        int first = ctr;
+        row[i] = ctr;
+        for (int j = nteIndex[i]; j < nteIndex[i + 1]; j++) {
+            long e = nteValue[j];
+            for (int k = 0; k < DIM_ELEM; k++) {
+                int nb = elemToNode[e * DIM_ELEM + k];
+                int isNew = 1;
+                for (int l = first; l < ctr; l++)
+                    if (col[l] == nb) { isNew = 0; break; }
+                if (isNew) col[ctr++] = nb;
+            }
+        }
+    }
+    row[nbNodes] = ctr;
+}
+
+void orc_create_elemToEdge(const int *row, const int *col, const int *elemToNode,
+                           int *elemToEdge, int nbElem)
+{
+    for (long i = 0; i < nbElem; i++) {
+        int ctr = 0;
+        for (int j = 0; j < DIM_ELEM; j++) {
+            int n1 = elemToNode[i * DIM_ELEM + j] - 1;
+            for (int k = 0; k < DIM_ELEM; k++) {
+                int n2 = elemToNode[i * DIM_ELEM + k];
+                for (int l = row[n1]; l < row[n1 + 1]; l++)
+                    if (col[l] == n2) { elemToEdge[i * 16 + ctr++] = l; break; }
+            }
+        }
+    }
+}
+
+static void orc_assemble_elem(const double *coord, double *values, const int *row,
+                              const int *col, const int *elemToNode, long elem,
+                              int operatorDim, int operatorID, const double *coef)
+{
+    double g[DIM_ELEM][DIM_NODE];
+    orc_elem_coef(g, coord, elemToNode, elem);
+    orc_coef_t c = orc_coef(coef, operatorID, elem);
+    for (int j = 0; j < DIM_ELEM; j++) {
+        int n1 = elemToNode[elem * DIM_ELEM + j] - 1;
+        for (int k = 0; k < DIM_ELEM; k++) {
+            int n2 = elemToNode[elem * DIM_ELEM + k];
+            for (int l = row[n1]; l < row[n1 + 1]; l++) {
+                if (col[l] == n2) {
+                    orc_add_block(values + (long)l * operatorDim, g[j], g[k], operatorID, &c);
+                    break;
+                }
+            }
+        }
+    }
+}
+
+void orc_assembly(const double *coord, double *values, const int *row, const int *col,
+                  const int *elemToNode, int nbElem, int nbEdges, int operatorDim,
+                  int operatorID, const double *coef)
+{
+    for (long i = 0; i < (long)nbEdges * operatorDim; i++) values[i] = 0;
+    for (long e = 0; e < nbElem; e++)
+        orc_assemble_elem(coord, values, row, col, elemToNode, e, operatorDim,
+                          operatorID, coef);
+}
+
+void orc_assembly_positions(const double *coord, double *values, const int *elemToEdge,
+                            const int *elemToNode, int nbElem, int nbEdges,
+                            int operatorDim, int operatorID, const double *coef)
+{
+    for (long i = 0; i < (long)nbEdges * operatorDim; i++) values[i] = 0;
+    for (long e = 0; e < nbElem; e++) {
+        double g[DIM_ELEM][DIM_NODE];
+        orc_elem_coef(g, coord, elemToNode, e);
+        orc_coef_t c = orc_coef(coef, operatorID, e);
+        for (int j = 0; j < DIM_ELEM; j++)
+            for (int k = 0; k < DIM_ELEM; k++) {
+                long p = elemToEdge[e * 16 + j * 4 + k];
+                orc_add_block(values + p * operatorDim, g[j], g[k], operatorID, &c);
+            }
+    }
+}
+
+void orc_assembly_ordered(const double *coord, double *values, const int *row,
+                          const int *col, const int *elemToNode, const int *order,
+                          int nbElem, int nbEdges, int operatorDim, int operatorID,
+                          const double *coef)
+{
+    for (long i = 0; i < (long)nbEdges * operatorDim; i++) values[i] = 0;
+    for (long i = 0; i < nbElem; i++)
+        orc_assemble_elem(coord, values, row, col, elemToNode, order[i], operatorDim,
+                          operatorID, coef);
+}
+
+void orc_prec_init(double *prec, const double *values, const int *row, const int *col,
+                   int nbNodes, int operatorDim)
+{
+    for (long i = 0; i < (long)nbNodes * operatorDim; i++) prec[i] = 0;
+    for (long i = 0; i < nbNodes; i++) {
+        for (int j = row[i]; j < row[i + 1]; j++) {
+            if (col[j] - 1 == i) {
+                for (int k = 0; k < operatorDim; k++)
+                    prec[i * operatorDim + k] = values[(long)j * operatorDim + k];
+                break;
+            }
+        }
+    }
+}
+
+void orc_ela_invert_prec(int nspa, int nnt, const int *innv, const int *nnv,
+                         double *prec, int *ier, const int *markf, int i)
+{
+    /* prec(nspa,nspa,nnt), column-major: prec(ki,kj,i) = P[(ki-1) + nspa*(kj-1)] */
+    double *P = prec + (long)(i - 1) * nspa * nspa;
+    for (int ki = 1; ki <= nspa; ki++) {
+        if (markf[(long)(i - 1) + (long)(ki - 1) * nnt] != 0) {
+            for (int kj = 1; kj <= nspa; kj++) {
+                P[(ki - 1) + nspa * (kj - 1)] = 0.0;
+                P[(kj - 1) + nspa * (ki - 1)] = 0.0;
+            }
+            P[(ki - 1) + nspa * (ki - 1)] = 1.0;
+        }
+    }
+    int found = 0;
+    for (int m = innv[i - 1] + 1; m <= innv[i]; m++)
+        if (nnv[m - 1] == i) { found = 1; break; }
+    if (!found) return;
+    double a[9];
+    int ipiv[3], info;
+    for (int k = 0; k < 9; k++) a[k] = P[k];
+    info = orc_dgetrf3(a, ipiv);
+    if (info != 0) *ier = info;
+    info = orc_dgetri3(a, ipiv);
+    if (info != 0) *ier = info;
+    for (int k = 0; k < 9; k++) P[k] = a[k];
+}
+
+int orc_prec_inversion(double *prec, const int *row, const int *col,
+                       const int *checkBounds, int nbNodes, int operatorID)
+{
+    int nbad = 0;
+    for (int i = 0; i < nbNodes; i++) {
+        if (operatorID == 0) {
+            prec[i] = 1.0 / prec[i];
+        } else {
+            int err = 0;
+            orc_ela_invert_prec(DIM_NODE, nbNodes, row, col, prec, &err, checkBounds, i + 1);
+            if (err != 0) nbad++;
+        }
+    }
+    return nbad;
+}
+
+void orc_dqmrd4(int nnt, const int *jlog, int *nnd, int *nlim, int *ier)
+{
+    int nndx = *nnd;
+    *ier = 0;
+    *nnd = 0;
+    for (int i = 1; i <= nnt; i++) {
+        if (jlog[i - 1] != 0) {
+            (*nnd)++;
+            if (*nnd <= nndx) nlim[*nnd - 1] = i;
+        }
+    }
+    if (*nnd > nndx) *ier = -1;
+}
+
+void orc_e_essbcm(int ndim, int nbp, int nnd, const int *nlim, const int *jlog,
+                  int *markf)
+{
+    for (long k = 0; k < (long)nbp * ndim; k++) markf[k] = 0;
+    for (int I = 0; I < nnd; I++) {
+        long nl = nlim[I] - 1;
+        int J = jlog[nl];
+        if (ndim == 2) {
+            if (J == 52) markf[nl] = 1;
+            else if (J == 54) markf[nl + nbp] = 1;
+            else { markf[nl] = 1; markf[nl + nbp] = 1; }
+        } else if (ndim == 3) {
+            if (J == 52) markf[nl] = 1;
+            else if (J == 53) markf[nl + nbp] = 1;
+            else if (J == 54) markf[nl + 2L * nbp] = 1;
+            else { markf[nl] = 1; markf[nl + nbp] = 1; markf[nl + 2L * nbp] = 1; }
+        }
+    }
+}
+
+int orc_coloring(const int *elemToNode, int nbElem, int nbNodes, int *colorPart,
+                 int *colorToElem)
+{
+    int *idx = (int *)malloc(sizeof(int) * ((size_t)nbNodes + 1));
+    int *val = (int *)malloc(sizeof(int) * (size_t)nbElem * DIM_ELEM);
+    orc_node_to_elem(nbNodes, nbElem, elemToNode, idx, val);
+    /* 128-bit colour masks as two 64-bit words (coloring.cc:47-76) */
+    unsigned long long *mask = (unsigned long long *)calloc((size_t)nbElem * 2, 8);
+    int nbColors = 0, ok = 1;
+    for (long e = 0; e < nbElem && ok; e++) {
+        unsigned long long lo = 0, hi = 0;
+        for (int k = 0; k < DIM_ELEM; k++) {
+            int n = elemToNode[e * DIM_ELEM + k] - 1;
+            for (int j = idx[n]; j < idx[n + 1]; j++) {
+                long f = val[j];
+                if (f == e) continue;
+                lo |= mask[2 * f];
+                hi |= mask[2 * f + 1];
+            }
+        }
+        int color = 0;
+        while (color < 128 && ((color < 64 ? (lo >> color) : (hi >> (color - 64))) & 1ULL))
+            color++;
+        if (color >= 128) { ok = 0; break; }
+        if (color < 64) mask[2 * e] = 1ULL << color;
+        else mask[2 * e + 1] = 1ULL << (color - 64);
+        colorPart[e] = color;
+        if (color > nbColors) nbColors = color;
+    }
+    free(mask); free(idx); free(val);
+    if (!ok) return -1;
+    nbColors++;
+    /* fill_color_index (coloring.cc:27-42) */
+    int *count = (int *)calloc((size_t)nbColors, sizeof(int));
+    for (long e = 0; e < nbElem; e++) count[colorPart[e]]++;
+    colorToElem[0] = 0;
+    for (int c = 1; c <= nbColors; c++) colorToElem[c] = colorToElem[c - 1] + count[c - 1];
+    free(count);
+    return nbColors;
+}
+
+double orc_norm(const double *x, long n)
+{
+    double s = 0;
+    for (long i = 0; i < n; i++) s += x[i] * x[i];
+    return sqrt(s);
+}
+
+int orc_getrf_getri3(double *a)
+{
+    int ipiv[3];
+    int i1 = orc_dgetrf3(a, ipiv);
+    int i2 = orc_dgetri3(a, ipiv);
+    return i1 ? i1 : i2;
+}
