@@ -1,0 +1,372 @@
+"""Benchmark: elasticity assembly + block-Jacobi preconditioner of the 100^3-node
+jittered, node-permuted Kuhn cube (1,000,000 nodes, 5,821,794 tets,
+14,761,198 CSR entries of 3x3 blocks) with per-element E and nu, one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one assembly + prec_init + prec_inversion of the whole mesh (what one
+iteration of the reference's FEM loop times, src/FEM.cc:177-234).  `value` is
+the FP32 path (FP32 arithmetic and values, Kahan-compensated sums, FP64
+slivers and block inversion) with inputs resident in HBM; the plain FP64
+bit-exact path is reported beside it (`fp64_plain`).  `e2e` runs the same FP32
+step through the C ABI with host buffers: coordinates and coefficients copied
+in, values and preconditioner copied out, every step.  The L2 cache (129 MB) is
+flushed before every timed step by writing a 512 MB buffer; each step is timed
+alone with CUDA events on the library's stream.
+
+--impl reference times the oracle port of the reference's CPU path (serial, as
+the reference's REF build is) on the same mesh; it is the reported baseline.
+With N > 1 (torchrun) every rank assembles its own mesh (weak scaling, no
+exchange: the preconditioner halo sum is a no-op at one rank per domain).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "mini-fem_gb300"))
+
+import numpy as np  # noqa: E402
+
+N_SIDE = 100
+SEED = 2024
+WORKLOAD = "ela_cube100_5.8M_tets"
+METRIC = "ela assembly Melem/s @5.8M tets: FP32-batched vs FP64-plain; % HBM roofline"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nme, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nme)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def step_bytes(E, N, nnz, fp32):
+    """Algorithmic bytes of one assembly + preconditioner step (ela):
+    16E connectivity + 3N coordinates + E coefficients + 64E (16 CSR positions
+    per element) + nnz*9 values + N*9*8 preconditioner."""
+    w = 4 if fp32 else 8
+    c = 8 if fp32 else 16
+    return 16 * E + 3 * N * w + c * E + 64 * E + nnz * 9 * w + N * 9 * 8
+
+
+def kernel_bytes(name, E, N, nnz, n_edge_units, fp32):
+    """Algorithmic bytes of one launch of the named kernel: its inputs read once
+    and its outputs written once."""
+    rec = 64 if fp32 else 128
+    w = 4 if fp32 else 8
+    contrib_edge = 6 * E
+    if name.startswith("edge_units"):
+        return (n_edge_units * (8 + 8) + 4 * contrib_edge + rec * E
+                + 2 * n_edge_units * 9 * w)
+    if name.startswith("diag_units"):
+        b = N * (4 + 8) + 4 * 4 * E + rec * E + N * 9 * w
+        if "prec" in name:
+            b += N * 9 * 8 + N
+        return b
+    if name.startswith("grad"):
+        coordb = 32 * N if fp32 else 24 * N
+        return 16 * E + coordb + (8 if fp32 else 16) * E + rec * E
+    return None
+
+
+def make_mesh(rank):
+    from minifem.meshgen import cube_mesh
+    return cube_mesh(N_SIDE, seed=SEED + rank, op="ela")
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import minifem
+    import pyoracle as O  # noqa: F401  (only for checkBounds + the CPU baseline leg)
+
+    torch.cuda.set_device(local_rank)
+    mesh = make_mesh(rank)
+    E, N = mesh.nbElem, mesh.nbNodes
+    a = minifem.Assembler(local_rank)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    nnz = len(col)
+    a.set_coefficients("ela", mesh.coef)
+    markf = O.checkbounds(mesh.boundNodesCode)
+    a.set_check_bounds(markf)
+    stream = torch.cuda.ExternalStream(a.stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+
+    def timed(precision, steps, warmup, e2e=False, hostbuf=None):
+        for _ in range(warmup):
+            one(precision, e2e, hostbuf)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        evs = []
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+            one(precision, e2e, hostbuf)
+            with torch.cuda.stream(stream):
+                e.record(stream)
+            evs.append((s, e))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if world > 1:
+            torch.distributed.barrier()
+        ms = [s.elapsed_time(e) for s, e in evs]
+        return ms, wall
+
+    def one(precision, e2e, hb):
+        if not e2e:
+            a.assembly("ela", precision, "gather", prec=True)
+            return
+        # host buffers in, host buffers out, through the C ABI
+        a.update_coords(hb["coord"])
+        a.set_coefficients("ela", hb["coef"])
+        a.assembly("ela", precision, "gather", prec=True)
+        minifem._native.lib.mfem_get_values_f32(a._h, hb["vals"].ctypes.data_as(minifem.api.C.c_void_p))
+        minifem._native.lib.mfem_get_prec(a._h, hb["prec"].ctypes.data_as(minifem.api.C.c_void_p))
+
+    # pinned host buffers for the end-to-end leg
+    pin = lambda arr: torch.from_numpy(arr).pin_memory().numpy()  # noqa: E731
+    hb = {"coord": pin(np.ascontiguousarray(mesh.coord)), "coef": pin(np.ascontiguousarray(mesh.coef)),
+          "vals": pin(np.empty(nnz * 9, np.float32)), "prec": pin(np.empty(N * 9, np.float64))}
+
+    with ClockSampler(local_rank) as clk:
+        ms32, _ = timed("fp32", args.steps, args.warmup)
+        ms64, _ = timed("fp64", args.steps, args.warmup)
+    e2e_ms, e2e_wall = timed("fp32", args.steps, max(1, args.warmup // 2), e2e=True, hostbuf=hb)
+
+    # per-kernel durations (a separate, untimed pass with events per launch)
+    prof = {}
+    for prec in ("fp32", "fp64"):
+        a.profile(True)
+        for _ in range(3):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            a.assembly("ela", prec, "gather", prec=True)
+        rec = a.profile_read()
+        a.profile(False)
+        agg = {}
+        for nme, t in rec:
+            agg.setdefault(nme, []).append(t)
+        prof[prec] = {k: sum(v) / len(v) for k, v in agg.items()}
+    flagged = a.flagged()
+
+    # maximum over ranks
+    t32 = statistics.mean(ms32)
+    t64 = statistics.mean(ms64)
+    te2e = statistics.mean(e2e_ms)
+    if world > 1:
+        t = torch.tensor([t32, t64, te2e], device=f"cuda:{local_rank}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t32, t64, te2e = t.tolist()
+    if rank != 0:
+        return None
+
+    hbm, peak_kind = peaks()
+    # edge units: upper off-diagonal entries
+    n_edge = (nnz - N) // 2
+
+    def roofline(prec, step_ms):
+        fp32 = prec == "fp32"
+        ks = prof[prec]
+        dom = max(ks, key=ks.get)
+        kb = kernel_bytes(dom, E, N, nnz, n_edge, fp32)
+        ach = kb / (ks[dom] * 1e-3) / 1e9
+        sb = step_bytes(E, N, nnz, fp32)
+        return ({"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm,
+                 "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
+                 "algorithmic_bytes": kb, "launch_ms": round(ks[dom], 4),
+                 "peak_kind": peak_kind},
+                {"algorithmic_bytes": sb, "GB/s": round(sb / (step_ms * 1e-3) / 1e9, 1),
+                 "frac": round(sb / (step_ms * 1e-3) / 1e9 / hbm, 4)})
+
+    r32, s32 = roofline("fp32", t32)
+    r64, s64 = roofline("fp64", t64)
+    melem = lambda ms: world * E / (ms * 1e-3) / 1e6  # noqa: E731
+    out = {
+        "metric": METRIC, "value": round(melem(t32), 1), "unit": "Melem/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t32, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: jittered (+-0.2h), node-permuted 100^3 Kuhn cube, E log-uniform "
+                "[1e9,2e11], nu U[0.2,0.35], seeded",
+        "config": {"workload": WORKLOAD, "nbElem": E, "nbNodes": N, "nbEdges": nnz,
+                   "operator": "ela", "precision": "fp32 (Kahan sums, fp64 slivers + block inverse)",
+                   "strategy": "gather", "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": r32, "step_roofline": s32,
+        "fp64_plain": {"value": round(melem(t64), 1), "unit": "Melem/s", "ms_per_step": round(t64, 4),
+                       "bit_exact": "gather, -fmad=false", "roofline": r64, "step_roofline": s64},
+        "fp32_over_fp64": round(t64 / t32, 2),
+        "kernels_ms": prof,
+        "flagged_slivers": flagged,
+        "e2e": {"value": round(melem(te2e), 1), "unit": "Melem/s", "ms_per_step": round(te2e, 4),
+                "h2d_bytes_per_step": int(hb["coord"].nbytes + hb["coef"].nbytes),
+                "d2h_bytes_per_step": int(hb["vals"].nbytes + hb["prec"].nbytes),
+                "path": "C ABI: mfem_update_coords + mfem_set_coefficients + mfem_assemble_prec"
+                        " + mfem_get_values_f32 + mfem_get_prec (pinned host buffers)"},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    # own kernels launched per timed step (fp32 step: split, coef, grad, diag, edge)
+    out["gpu_launches"] = 5 * args.steps
+    if args.cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(mesh, row, col, markf, args.cpu_iters)
+    a.close()
+    return out
+
+
+def cpu_baseline(mesh, row, col, markf, iters):
+    """Oracle port of the reference's REF path (serial), timed on this host."""
+    import pyoracle as O
+    E, N = mesh.nbElem, mesh.nbNodes
+    # the port's own pattern (reference column order), as the reference builds it
+    prow, pcol = O.pattern(mesh.elemToNode, N)
+    nnz = int(prow[-1])
+    t = []
+    for _ in range(iters):
+        t0 = time.perf_counter()
+        vals = O.assembly(mesh.coord, prow, pcol, mesh.elemToNode, nnz, "ela", mesh.coef)
+        O.prec(vals, prow, pcol, markf, N, "ela")
+        t.append(time.perf_counter() - t0)
+    sec = statistics.mean(t)
+    return {"value": round(E / sec / 1e6, 3), "unit": "Melem/s", "cores": 1, "kind": "port",
+            "sample": f"{iters} full iterations (assembly + prec_init + prec_inversion) of the "
+                      f"same 5.8M-tet mesh, {sec:.2f} s each"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import pyoracle as O
+    mesh = make_mesh(0)
+    E, N = mesh.nbElem, mesh.nbNodes
+    row, col = O.pattern(mesh.elemToNode, N)
+    nnz = int(row[-1])
+    markf = O.checkbounds(mesh.boundNodesCode)
+
+    def step():
+        vals = O.assembly(mesh.coord, row, col, mesh.elemToNode, nnz, "ela", mesh.coef)
+        O.prec(vals, row, col, markf, N, "ela")
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    sec = (time.perf_counter() - t0) / args.steps
+    v = round(E / sec / 1e6, 3)
+    return {"metric": METRIC, "value": v, "unit": "Melem/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nbElem": E, "nbNodes": N, "nbEdges": nnz},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "Melem/s", "cores": 1, "kind": "port",
+                             "sample": "full mesh per step; the reference's REF path is serial "
+                                       "(its COLORING build disables the per-element pragma, "
+                                       "src/assembly.cc:362,516)"},
+            "e2e": {"value": v, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--cpu-iters", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if args.impl == "ours":
+            torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group(backend)
+    try:
+        if args.impl == "reference":
+            out = run_reference(args, rank, world)
+        else:
+            out = run_ours(args, rank, world, local_rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

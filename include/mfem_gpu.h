@@ -1,0 +1,163 @@
+/* mfem_gpu.h — C ABI of the GB300 (sm_103a) implementation of Mini-FEM's
+ * assembly step: CSR pattern, element colouring, Laplacian / 3-DOF elasticity
+ * assembly of P1 tetrahedra and block-Jacobi preconditioner creation.
+ *
+ * Plain C types only (pointers and sizes); every function returns an int status
+ * (MFEM_OK = 0, negative on failure; mfem_last_error() gives the message).
+ * Index conventions are the reference's: elemToNode and CSR columns 1-based,
+ * CSR row pointers 0-based (src/matrix.cc:55-91, src/main.cc:243-249).
+ * Unless a name ends in _device, pointer arguments are HOST memory.
+ *
+ * Each entry point names the reference interface it replaces.  The reference
+ * operators return void and exit(EXIT_FAILURE) on error
+ * (src/coloring.cc:66-69, src/IO.cc:33-36); here the status is returned and the
+ * caller decides (include/minifem_dropin.h keeps the exit behaviour).
+ */
+#ifndef MFEM_GPU_H
+#define MFEM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFEM_ABI_VERSION 1
+
+/* status codes */
+#define MFEM_OK               0
+#define MFEM_ERR_INVALID_ARG (-1)
+#define MFEM_ERR_CUDA        (-2)
+#define MFEM_ERR_NO_DEVICE   (-3)
+#define MFEM_ERR_STATE       (-4)  /* call out of order (e.g. assemble before a mesh) */
+#define MFEM_ERR_PATTERN     (-5)  /* nbEdges / pattern mismatch, row too long */
+#define MFEM_ERR_COLORS      (-6)  /* more than 128 colours (src/coloring.cc:66-69) */
+#define MFEM_ERR_CAPACITY    (-7)  /* caller buffer or fixed limit too small */
+#define MFEM_ERR_TIMEOUT     (-8)  /* a bounded device wait gave up */
+
+/* operatorID (src/main.cc:131-138) */
+#define MFEM_OP_LAP 0
+#define MFEM_OP_ELA 1
+
+/* precision */
+#define MFEM_FP64 0   /* FP64 arithmetic and values */
+#define MFEM_FP32 1   /* FP32 element arithmetic and values, compensated sums,
+                         FP64 for flagged slivers and the block inversion */
+
+/* strategy */
+#define MFEM_AUTO    (-1)
+#define MFEM_GATHER    0  /* owner-computes, ascending element order (bit-exact FP64) */
+#define MFEM_SCATTER   1  /* colour-ordered scatter, no atomics */
+#define MFEM_ATOMIC    2  /* element-parallel atomics (order not deterministic) */
+
+/* column order of the CSR pattern */
+#define MFEM_ORDER_SORTED    0  /* ascending columns in each row */
+#define MFEM_ORDER_REFERENCE 1  /* first occurrence, as src/matrix.cc:55-91 */
+
+typedef struct mfem_context mfem_context;
+
+/* ---- lifecycle ------------------------------------------------------------ */
+int mfem_create(mfem_context **ctx, int device);
+int mfem_destroy(mfem_context *ctx);
+const char *mfem_last_error(const mfem_context *ctx);
+const char *mfem_status_string(int status);
+int mfem_abi_version(void);
+/* The CUDA stream every call of this context is ordered on (cudaStream_t). */
+int mfem_get_stream(mfem_context *ctx, void **stream);
+
+/* ---- mesh (src/IO.cc:61-96 arrays) ----------------------------------------- */
+/* Uploads coord[nbNodes*3] and elemToNode[nbElem*4] (1-based).  Replaces the
+ * mesh and drops every structure built on the previous one. */
+int mfem_set_mesh(mfem_context *ctx, const double *coord, const int *elemToNode,
+                  int nbElem, int nbNodes);
+/* New coordinates for the same topology (keeps pattern, colouring, plans). */
+int mfem_update_coords(mfem_context *ctx, const double *coord);
+
+/* ---- CSR pattern: replaces create_nodeToNode (src/matrix.cc:55-91, called at
+ * src/main.cc:247-249) and create_elemToEdge (src/matrix.cc:25-52). ---------- */
+/* Builds the pattern on the device.  row[nbNodes+1] and col[capacity] may be
+ * NULL (device-only).  *nbEdges receives nnz.  MFEM_ERR_CAPACITY if
+ * capacity < nnz (nothing written to col then). */
+int mfem_create_nodeToNode(mfem_context *ctx, int order, int *row, int *col,
+                           int capacity, int *nbEdges);
+/* elemToEdge[nbElem*16]: 0-based CSR position of (j,k), j-major. */
+int mfem_create_elemToEdge(mfem_context *ctx, int *elemToEdge);
+/* Adopts a pattern the caller built (row 0-based, col 1-based, any column order).
+ * Every element pair must be present: MFEM_ERR_PATTERN otherwise. */
+int mfem_set_pattern(mfem_context *ctx, const int *row, const int *col, int nbEdges);
+
+/* ---- colouring: replaces coloring_creation (src/coloring.cc:84-109) --------- */
+/* Jones-Plassmann first-fit colouring of the element graph on the device
+ * (elements sharing a node get different colours), at most 128 colours.
+ * colorPerm[nbElem] (may be NULL): colorPerm[old] = position in colour order
+ * (stable), the convention src/main.cc:229 applies; colorIndex[nbColors+1]
+ * (may be NULL, capacity entries).  The colouring is used by MFEM_SCATTER. */
+int mfem_coloring_creation(mfem_context *ctx, unsigned long long seed, int *colorPerm,
+                           int *colorIndex, int capacity, int *nbColors);
+
+/* ---- assembly: replaces assembly (src/assembly.cc:615-720) ------------------ */
+/* coef == NULL: the reference operator (constants 1 / 2.25, 1.25).  Otherwise
+ * lap: kappa[nbElem]; ela: (E, nu)[nbElem*2], Young's modulus and Poisson ratio
+ * per element, weighted as lambda = E nu / ((1+nu)(1-2nu)), mu = E / (2(1+nu)). */
+int mfem_set_coefficients(mfem_context *ctx, int operatorID, const double *coef);
+/* Assembles nodeToNodeValue on the device (kept there).  Enqueued on the
+ * context stream; returns without waiting. */
+int mfem_assemble(mfem_context *ctx, int operatorID, int precision, int strategy);
+
+/* ---- preconditioner: replaces prec_init (src/preconditioner.cc:52-87) and
+ * prec_inversion (src/preconditioner.cc:25-49, src/Fortran/elasclpr.f). ------ */
+/* checkBounds[nbNodes*3], column-major MARKF(nbNodes,3) as e_essbcm_ builds it
+ * (src/main.cc:340-346).  NULL means no Dirichlet DOF. */
+int mfem_set_check_bounds(mfem_context *ctx, const int *checkBounds);
+int mfem_prec_init(mfem_context *ctx);
+/* *nbSingular (may be NULL) receives the number of blocks whose LU hit an exact
+ * zero pivot (the reference prints "info[DGETRF]" and carries on). Synchronises. */
+int mfem_prec_inversion(mfem_context *ctx, int *nbSingular);
+/* assembly + prec_init + prec_inversion in one enqueue (prec fused into the
+ * assembly kernels where the strategy allows). */
+int mfem_assemble_prec(mfem_context *ctx, int operatorID, int precision, int strategy);
+
+/* FP32 precision: elements whose shape quality |6V| / (|a| |b| |c|) (a, b, c the
+ * edge vectors from the fourth node) is below `threshold` are integrated in FP64
+ * (default 0.05).  *nbFlagged receives the count of the last FP32 assembly. */
+int mfem_set_sliver_threshold(mfem_context *ctx, double threshold);
+int mfem_get_flagged(mfem_context *ctx, int *nbFlagged);
+
+/* ---- results ---------------------------------------------------------------- */
+int mfem_get_values(mfem_context *ctx, double *values);     /* nbEdges*opDim, FP64 */
+int mfem_get_values_f32(mfem_context *ctx, float *values);  /* FP32 assembly only */
+int mfem_get_prec(mfem_context *ctx, double *prec);         /* nbNodes*opDim */
+/* Device addresses of the results (valid until the next mesh/pattern change). */
+int mfem_values_device(mfem_context *ctx, void **values, int *precision);
+int mfem_prec_device(mfem_context *ctx, double **prec);
+int mfem_synchronize(mfem_context *ctx);
+/* Per-kernel timing with CUDA events on the context stream (no counterpart in
+ * the reference, whose DC_timer brackets whole steps, src/FEM.cc:182-233).
+ * mfem_profile_read synchronises, returns the named regions recorded since
+ * the last read ("name;name;..." in names) with their durations in ms, and
+ * clears the list. */
+int mfem_profile(mfem_context *ctx, int enable);
+int mfem_profile_read(mfem_context *ctx, char *names, int namesCap, float *ms, int cap,
+                      int *count);
+/* Sizes: nbElem, nbNodes, nbEdges, nbColors (any pointer may be NULL). */
+int mfem_get_sizes(mfem_context *ctx, int *nbElem, int *nbNodes, int *nbEdges,
+                   int *nbColors);
+
+/* ---- reference-shaped single calls (host buffers in and out) ---------------- */
+/* Same arguments and meaning as the reference operators; each call uploads what
+ * it reads and downloads what it writes.  nodeToNodeRow / nodeToNodeColumn must
+ * describe the pattern (either the one mfem_create_nodeToNode returned, which is
+ * recognised without re-upload, or any valid CSR of the mesh). */
+int mfem_assembly(mfem_context *ctx, double *coord, double *nodeToNodeValue,
+                  int *nodeToNodeRow, int *nodeToNodeColumn, int *elemToNode,
+                  int *elemToEdge, int nbElem, int nbEdges, int operatorDim,
+                  int operatorID);
+int mfem_prec_init_host(mfem_context *ctx, double *prec, double *nodeToNodeValue,
+                        int *nodeToNodeRow, int *nodeToNodeColumn, int nbNodes,
+                        int operatorDim);
+int mfem_prec_inversion_host(mfem_context *ctx, double *prec, int *nodeToNodeRow,
+                             int *nodeToNodeColumn, int *checkBounds, int nbNodes,
+                             int operatorID);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

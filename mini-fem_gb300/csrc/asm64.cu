@@ -1,0 +1,407 @@
+// FP64 assembly and preconditioner kernels (built with -fmad=false).
+//
+// Replaces assembly() (src/assembly.cc:615-720: reset + assembly_{lap,ela}_seq),
+// prec_init (src/preconditioner.cc:52-87) and prec_inversion
+// (src/preconditioner.cc:25-49 with src/Fortran/elasclpr.f).
+//
+// Strategies:
+//  * GATHER (owner computes, deterministic): k_grad64 writes one 128-byte
+//    gradient record per element; k_diag_units64 / k_edge_units64 then sum, for
+//    every upper CSR entry, its element contributions in ascending element order
+//    starting from 0.0 -- the reference REF build's summation order -- and write
+//    the entry and its transpose.  Bit-exact with the reference under
+//    -fmad=false.  The diagonal kernel can also fuse prec_init + prec_inversion.
+//  * SCATTER (colour order, no atomics): one launch per colour; each element
+//    adds its 16 blocks into the values it owns within the colour.
+//  * ATOMIC: one launch, FP64 atomic adds (summation order not deterministic).
+#include "context.h"
+#include "elem_math.cuh"
+
+namespace mfem {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ double fix_zero(double x) {
+    // 0.0 + x: identical to x except that -0.0 becomes +0.0 (integer pipe)
+    const long long b = __double_as_longlong(x);
+    return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
+}
+
+template <int OP, bool COEF>
+__global__ void __launch_bounds__(kThreads)
+k_grad64(const double *__restrict__ coord, const int4 *__restrict__ e2n,
+         const double *__restrict__ coef, int nbElem, double *__restrict__ rec) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nbElem) return;
+    double g[12];
+    elem_gradients(coord, e2n[e], g);
+    double2 *out = reinterpret_cast<double2 *>(rec + (size_t)e * kRec64);
+#pragma unroll
+    for (int i = 0; i < 6; i++) out[i] = make_double2(g[2 * i], g[2 * i + 1]);
+    if (COEF) {
+        if (OP == MFEM_OP_LAP) {
+            out[6] = make_double2(coef[e], 0.0);
+        } else {
+            double A, B, mu;
+            lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
+            out[6] = make_double2(A, B);
+            out[7] = make_double2(mu, 0.0);
+        }
+    }
+}
+
+__device__ __forceinline__ void load3(const double *p, double *g) {
+    g[0] = p[0];
+    g[1] = p[1];
+    g[2] = p[2];
+}
+
+// Diagonal units: entry (r, r) = sum over incident elements (ascending) of
+// block (j, j).  Optionally fused with prec_init + prec_inversion.
+template <int OP, bool COEF, bool PREC>
+__global__ void __launch_bounds__(kThreads)
+k_diag_units64(const int *__restrict__ diagPos, const int *__restrict__ start,
+               const unsigned *__restrict__ contrib, const double *__restrict__ rec,
+               int nbNodes, double *__restrict__ values, double *__restrict__ prec,
+               const unsigned char *__restrict__ mask, int *singular) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    const int p = diagPos[r];
+    if (OP == MFEM_OP_LAP) {
+        double acc = 0.0;
+        if (p >= 0) {
+            const int b = start[p], en = start[p + 1];
+            for (int q = b; q < en; q++) {
+                const unsigned u = contrib[q];
+                const double *R = rec + (size_t)(u >> 4) * kRec64;
+                double g[3];
+                load3(R + 3 * ((u >> 2) & 3), g);
+                const double v = lap_entry<!COEF>(g, g, COEF ? R[12] : 1.0);
+                acc = (q == b) ? fix_zero(v) : acc + v;
+            }
+            values[p] = acc;
+        }
+        if (PREC) prec[r] = 1.0 / acc;
+        return;
+    }
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (p >= 0) {
+        const int b = start[p], en = start[p + 1];
+        for (int q = b; q < en; q++) {
+            const unsigned u = contrib[q];
+            const double *R = rec + (size_t)(u >> 4) * kRec64;
+            double g[3], d[6];
+            load3(R + 3 * ((u >> 2) & 3), g);
+            double A = 0.0, B = 0.0, mu = 0.0;
+            if (COEF) { A = R[12]; B = R[13]; mu = R[14]; }
+            ela_diag_block<!COEF>(g, A, B, mu, d);
+            if (q == b) {
+#pragma unroll
+                for (int m = 0; m < 6; m++) acc[m] = fix_zero(d[m]);
+            } else {
+#pragma unroll
+                for (int m = 0; m < 6; m++) acc[m] = acc[m] + d[m];
+            }
+        }
+        double *v = values + (size_t)p * 9;
+        v[0] = acc[0]; v[1] = acc[3]; v[2] = acc[4];
+        v[3] = acc[3]; v[4] = acc[1]; v[5] = acc[5];
+        v[6] = acc[4]; v[7] = acc[5]; v[8] = acc[2];
+    }
+    if (PREC) {
+        double a[9] = {acc[0], acc[3], acc[4], acc[3], acc[1], acc[5], acc[4], acc[5], acc[2]};
+        if (mask) dirichlet_mask3(a, mask[r]);
+        if (p >= 0) {
+            if (lu_inverse3(a) != 0) atomicAdd(singular, 1);
+        }
+        double *o = prec + (size_t)r * 9;
+#pragma unroll
+        for (int m = 0; m < 9; m++) o[m] = a[m];
+    }
+}
+
+// Upper off-diagonal units: entry (r, c), c > r, and its transpose (c, r).
+template <int OP, bool COEF>
+__global__ void __launch_bounds__(kThreads)
+k_edge_units64(const int2 *__restrict__ unitPos, int nUnits, const int *__restrict__ start,
+               const unsigned *__restrict__ contrib, const double *__restrict__ rec,
+               double *__restrict__ values) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nUnits) return;
+    const int2 pp = unitPos[t];
+    const int b = start[pp.x], en = start[pp.x + 1];
+    if constexpr (OP == MFEM_OP_LAP) {
+        double acc = 0.0;
+        for (int q = b; q < en; q++) {
+            const unsigned u = contrib[q];
+            const double *R = rec + (size_t)(u >> 4) * kRec64;
+            double gj[3], gk[3];
+            load3(R + 3 * ((u >> 2) & 3), gj);
+            load3(R + 3 * (u & 3), gk);
+            const double v = lap_entry<!COEF>(gj, gk, COEF ? R[12] : 1.0);
+            acc = (q == b) ? fix_zero(v) : acc + v;
+        }
+        values[pp.x] = acc;
+        values[pp.y] = acc;
+    } else {
+    double acc[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) acc[m] = 0.0;
+    for (int q = b; q < en; q++) {
+        const unsigned u = contrib[q];
+        const double *R = rec + (size_t)(u >> 4) * kRec64;
+        double gj[3], gk[3], c[9];
+        load3(R + 3 * ((u >> 2) & 3), gj);
+        load3(R + 3 * (u & 3), gk);
+        double A = 0.0, B = 0.0, mu = 0.0;
+        if (COEF) { A = R[12]; B = R[13]; mu = R[14]; }
+        ela_block<!COEF>(gj, gk, A, B, mu, c);
+        if (q == b) {
+#pragma unroll
+            for (int m = 0; m < 9; m++) acc[m] = fix_zero(c[m]);
+        } else {
+#pragma unroll
+            for (int m = 0; m < 9; m++) acc[m] = acc[m] + c[m];
+        }
+    }
+    double *v = values + (size_t)pp.x * 9;
+    double *w = values + (size_t)pp.y * 9;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int bb = 0; bb < 3; bb++) {
+            v[3 * a + bb] = acc[3 * a + bb];
+            w[3 * bb + a] = acc[3 * a + bb];
+        }
+    }
+}
+
+// ---- element-parallel strategies (scatter within a colour / atomics) ----------
+
+template <int OP, bool COEF, bool ATOMIC>
+__global__ void __launch_bounds__(kThreads)
+k_elem_scatter64(const int *__restrict__ elems, int count, const double *__restrict__ coord,
+                 const int4 *__restrict__ e2n, const double *__restrict__ coef,
+                 const int *__restrict__ elemPos, double *__restrict__ values) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int e = elems ? elems[t] : t;
+    double g[12];
+    elem_gradients(coord, e2n[e], g);
+    double A = 2.25, B = 1.25, mu = 1.0, kappa = 1.0;
+    if (COEF) {
+        if (OP == MFEM_OP_LAP) kappa = coef[e];
+        else lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
+    }
+    const int *pos = elemPos + (size_t)e * 16;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+#pragma unroll
+        for (int k = j; k < 4; k++) {
+            const int pjk = pos[4 * j + k], pkj = pos[4 * k + j];
+            if (OP == MFEM_OP_LAP) {
+                const double v = lap_entry<!COEF>(g + 3 * j, g + 3 * k, kappa);
+                if (ATOMIC) {
+                    atomicAdd(values + pjk, v);
+                    if (k != j) atomicAdd(values + pkj, v);
+                } else {
+                    values[pjk] = values[pjk] + v;
+                    if (k != j) values[pkj] = values[pkj] + v;
+                }
+            } else {
+                double c[9];
+                ela_block<!COEF>(g + 3 * j, g + 3 * k, A, B, mu, c);
+                double *vj = values + (size_t)pjk * 9;
+                double *vk = values + (size_t)pkj * 9;
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int bb = 0; bb < 3; bb++) {
+                        const double x = c[3 * a + bb];
+                        if (ATOMIC) {
+                            atomicAdd(vj + 3 * a + bb, x);
+                            if (k != j) atomicAdd(vk + 3 * bb + a, x);
+                        } else {
+                            vj[3 * a + bb] = vj[3 * a + bb] + x;
+                            if (k != j) vk[3 * bb + a] = vk[3 * bb + a] + x;
+                        }
+                    }
+            }
+        }
+    }
+}
+
+// ---- preconditioner (separate calls) ------------------------------------------
+
+__global__ void k_prec_init64(const double *__restrict__ values, const int *__restrict__ diagPos,
+                              int nbNodes, int dim, double *__restrict__ prec) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nbNodes * dim) return;
+    const int r = (int)(i / dim), k = (int)(i % dim);
+    const int p = diagPos[r];
+    prec[i] = p >= 0 ? values[(size_t)p * dim + k] : 0.0;
+}
+
+__global__ void k_prec_init32(const float *__restrict__ values, const int *__restrict__ diagPos,
+                              int nbNodes, int dim, double *__restrict__ prec) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nbNodes * dim) return;
+    const int r = (int)(i / dim), k = (int)(i % dim);
+    const int p = diagPos[r];
+    prec[i] = p >= 0 ? (double)values[(size_t)p * dim + k] : 0.0;
+}
+
+template <int OP>
+__global__ void k_prec_invert(double *__restrict__ prec, const int *__restrict__ diagPos,
+                              const unsigned char *__restrict__ mask, int nbNodes,
+                              int *singular) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    if (OP == MFEM_OP_LAP) {
+        prec[r] = 1.0 / prec[r];
+        return;
+    }
+    double a[9];
+    double *P = prec + (size_t)r * 9;
+#pragma unroll
+    for (int m = 0; m < 9; m++) a[m] = P[m];
+    if (mask) dirichlet_mask3(a, mask[r]);
+    if (diagPos[r] >= 0) {
+        if (lu_inverse3(a) != 0) atomicAdd(singular, 1);
+    }
+#pragma unroll
+    for (int m = 0; m < 9; m++) P[m] = a[m];
+}
+
+template <int OP, bool COEF>
+void launch_gather(Context &c, bool fusePrec) {
+    const GatherPlan &g = c.gather;
+    const int E = c.nbElem, N = c.nbNodes;
+    double *rec = (double *)c.grad.reserve(sizeof(double) * kRec64 * (size_t)E);
+    c.timer.begin("grad64", c.stream);
+    k_grad64<OP, COEF><<<blocks_for(E, kThreads), kThreads, 0, c.stream>>>(
+        c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(), E, rec);
+    check_launch("k_grad64");
+    c.timer.end(c.stream);
+    const int dim = OP == MFEM_OP_LAP ? 1 : 9;
+    double *vals = c.values.as<double>();
+    double *prec = fusePrec ? (double *)c.prec.reserve(sizeof(double) * (size_t)N * dim) : nullptr;
+    const unsigned char *mask = c.hasMask ? c.mask.as<unsigned char>() : nullptr;
+    int *sing = status_ptr(c) + 4;
+    if (fusePrec) MFEM_CUDA(cudaMemsetAsync(sing, 0, sizeof(int), c.stream));
+    c.timer.begin(fusePrec ? "diag_units64+prec" : "diag_units64", c.stream);
+    if (fusePrec)
+        k_diag_units64<OP, COEF, true><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(
+            c.diagPos.as<int>(), g.unitStart.as<int>(), g.contrib.as<unsigned>(), rec, N, vals,
+            prec, mask, sing);
+    else
+        k_diag_units64<OP, COEF, false><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(
+            c.diagPos.as<int>(), g.unitStart.as<int>(), g.contrib.as<unsigned>(), rec, N, vals,
+            prec, mask, sing);
+    check_launch("k_diag_units64");
+    c.timer.end(c.stream);
+    if (g.nUnits > 0) {
+        c.timer.begin("edge_units64", c.stream);
+        k_edge_units64<OP, COEF><<<blocks_for(g.nUnits, kThreads), kThreads, 0, c.stream>>>(
+            g.unitPos.as<int2>(), g.nUnits, g.unitStart.as<int>(), g.contrib.as<unsigned>(), rec,
+            vals);
+        check_launch("k_edge_units64");
+        c.timer.end(c.stream);
+    }
+}
+
+template <int OP, bool COEF>
+void launch_elementwise(Context &c, bool atomic) {
+    const int dim = OP == MFEM_OP_LAP ? 1 : 9;
+    double *vals = c.values.as<double>();
+    c.timer.begin(atomic ? "atomic64" : "scatter64", c.stream);
+    MFEM_CUDA(cudaMemsetAsync(vals, 0, sizeof(double) * (size_t)c.nnz * dim, c.stream));
+    if (atomic) {
+        k_elem_scatter64<OP, COEF, true><<<blocks_for(c.nbElem, kThreads), kThreads, 0, c.stream>>>(
+            nullptr, c.nbElem, c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(),
+            c.elemPos.as<int>(), vals);
+        check_launch("k_elem_scatter64<atomic>");
+        c.timer.end(c.stream);
+        return;
+    }
+    const Coloring &col = c.coloring;
+    for (int k = 0; k < col.nbColors; k++) {
+        const int b = col.hOffsets[k], n = col.hOffsets[k + 1] - b;
+        if (n <= 0) continue;
+        k_elem_scatter64<OP, COEF, false><<<blocks_for(n, kThreads), kThreads, 0, c.stream>>>(
+            col.colorElems.as<int>() + b, n, c.coord.as<double>(), c.e2n.as<int4>(),
+            c.coef.as<double>(), c.elemPos.as<int>(), vals);
+        check_launch("k_elem_scatter64<colour>");
+    }
+    c.timer.end(c.stream);
+}
+
+}  // namespace
+
+void assemble_fp64(Context &c, int op, int strategy, bool fusePrec) {
+    const bool coef = c.coefOp == op;
+    const int dim = op == MFEM_OP_LAP ? 1 : 9;
+    c.values.reserve(sizeof(double) * (size_t)c.nnz * dim);
+    if (strategy == MFEM_GATHER) {
+        build_gather_plan(c);
+        if (op == MFEM_OP_LAP) {
+            if (coef) launch_gather<MFEM_OP_LAP, true>(c, fusePrec);
+            else launch_gather<MFEM_OP_LAP, false>(c, fusePrec);
+        } else {
+            if (coef) launch_gather<MFEM_OP_ELA, true>(c, fusePrec);
+            else launch_gather<MFEM_OP_ELA, false>(c, fusePrec);
+        }
+    } else {
+        build_elem_pos(c);
+        const bool atomic = strategy == MFEM_ATOMIC;
+        MFEM_REQUIRE(atomic || c.coloring.built, MFEM_ERR_STATE,
+                     "scatter strategy needs mfem_coloring_creation first");
+        if (op == MFEM_OP_LAP) {
+            if (coef) launch_elementwise<MFEM_OP_LAP, true>(c, atomic);
+            else launch_elementwise<MFEM_OP_LAP, false>(c, atomic);
+        } else {
+            if (coef) launch_elementwise<MFEM_OP_ELA, true>(c, atomic);
+            else launch_elementwise<MFEM_OP_ELA, false>(c, atomic);
+        }
+    }
+    c.lastOp = op;
+    c.lastPrecision = MFEM_FP64;
+    c.precIsInit = fusePrec && strategy == MFEM_GATHER;
+}
+
+void prec_init_fp64(Context &c, int op) {
+    const int dim = op == MFEM_OP_LAP ? 1 : 9;
+    double *prec = (double *)c.prec.reserve(sizeof(double) * (size_t)c.nbNodes * dim);
+    const long long n = (long long)c.nbNodes * dim;
+    c.timer.begin("prec_init", c.stream);
+    if (c.lastPrecision == MFEM_FP64)
+        k_prec_init64<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.values.as<double>(),
+                                                                c.diagPos.as<int>(), c.nbNodes, dim, prec);
+    else
+        k_prec_init32<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.values.as<float>(),
+                                                                c.diagPos.as<int>(), c.nbNodes, dim, prec);
+    check_launch("k_prec_init");
+    c.timer.end(c.stream);
+}
+
+int prec_invert(Context &c, int op) {
+    int *sing = status_ptr(c) + 4;
+    MFEM_CUDA(cudaMemsetAsync(sing, 0, sizeof(int), c.stream));
+    const unsigned char *mask = c.hasMask ? c.mask.as<unsigned char>() : nullptr;
+    c.timer.begin("prec_invert", c.stream);
+    if (op == MFEM_OP_LAP)
+        k_prec_invert<MFEM_OP_LAP><<<blocks_for(c.nbNodes, kThreads), kThreads, 0, c.stream>>>(
+            c.prec.as<double>(), c.diagPos.as<int>(), mask, c.nbNodes, sing);
+    else
+        k_prec_invert<MFEM_OP_ELA><<<blocks_for(c.nbNodes, kThreads), kThreads, 0, c.stream>>>(
+            c.prec.as<double>(), c.diagPos.as<int>(), mask, c.nbNodes, sing);
+    check_launch("k_prec_invert");
+    c.timer.end(c.stream);
+    int h[5];
+    read_status(c, h, 5);
+    return h[4];
+}
+
+}  // namespace mfem

@@ -1,0 +1,120 @@
+// Device state of one mesh: inputs, CSR pattern, colouring, assembly plans and
+// results, all resident in HBM for the lifetime of the context.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace mfem {
+
+// Gather plan ("units").  A unit is one CSR entry (r, c) with c >= r in node
+// order; its transpose (c, r) receives the transposed block, which is bitwise
+// the same sum because block(k,j) = block(j,k)^T exactly and both entries see
+// the same elements in the same ascending order.  contrib lists every
+// (element, j, k) adding to the unit, ascending element id, packed
+// e << 4 | j << 2 | k.
+struct GatherPlan {
+    bool built = false;
+    int nUnits = 0;
+    long long nContrib = 0;
+    DevBuf unitStart;   // int [nUnits + 1]  offsets into contrib (in unit order)
+    DevBuf unitPos;     // int2[nUnits]      (pos(r,c), pos(c,r))
+    DevBuf contrib;     // u32 [nContrib]
+    int nDiagUnits = 0; // units [0, nDiagUnits) are diagonal entries
+    DevBuf diagNode;    // int [nDiagUnits]  node of each diagonal unit
+};
+
+struct Coloring {
+    bool built = false;
+    int nbColors = 0;
+    std::vector<int> hOffsets;   // nbColors + 1, into colorElems
+    DevBuf color;                // int [E]
+    DevBuf colorElems;           // int [E] elements sorted by colour (stable)
+};
+
+// Optional per-kernel CUDA-event timing (mfem_profile): each named launch
+// region is bracketed by two events on the context stream.
+struct KernelTimer {
+    bool on = false;
+    struct Rec { const char *name; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    size_t used = 0;
+    void begin(const char *name, cudaStream_t s);
+    void end(cudaStream_t s);
+    void reset() { used = 0; }
+    ~KernelTimer();
+};
+
+struct Context {
+    int device = 0;
+    KernelTimer timer;
+    cudaStream_t stream = nullptr;
+    std::string lastError;
+
+    // mesh
+    int nbElem = 0, nbNodes = 0;
+    DevBuf coord;      // double [N*3]
+    DevBuf e2n;        // int    [E*4], 0-based
+    const void *hostE2n = nullptr;   // identity of the caller's elemToNode
+
+    // pattern
+    bool hasPattern = false;
+    int nnz = 0, order = MFEM_ORDER_SORTED;
+    DevBuf rowPtr, col, diagPos;      // col 0-based
+    DevBuf nodeElemPtr, nodeElem;     // incidence, ascending element per node
+    bool hasIncidence = false;
+    DevBuf elemPos;                   // int [E*16]
+    bool hasElemPos = false;
+    const void *hostRow = nullptr, *hostCol = nullptr;  // identity of caller's CSR
+
+    GatherPlan gather;
+    Coloring coloring;
+
+    // coefficients
+    int coefOp = -1;                  // -1: reference constants
+    DevBuf coef;                      // double [E] or [E*2]
+
+    // Dirichlet mask, one byte per node: bit k = DOF k constrained
+    DevBuf mask;
+    bool hasMask = false;
+
+    // results
+    int lastOp = -1, lastPrecision = MFEM_FP64;
+    DevBuf values;                    // double or float [nnz * opDim]
+    DevBuf prec;                      // double [N * opDim]
+    bool precIsInit = false;
+
+    // FP32 path: elements whose quality |6V| / (|a||b||c|) is below this
+    // threshold get their Jacobian in FP64; the count of the last assembly is
+    // kept in status[5].
+    float sliverThreshold = 0.05f;
+    bool flaggedPending = false;
+
+    // scratch
+    DevBuf grad;                      // per-element gradient records
+    DevBuf scratch, scratch2, scanTmp;
+    DevBuf status;                    // int[8] device-side error flags
+};
+
+// pattern.cu
+void build_incidence(Context &c);
+void build_pattern(Context &c, int order);
+void adopt_pattern(Context &c, const int *hRow, const int *hCol, int nnz);
+void build_elem_pos(Context &c);
+void build_gather_plan(Context &c);
+
+// coloring.cu
+void build_coloring(Context &c, unsigned long long seed);
+
+// asm64.cu
+void assemble_fp64(Context &c, int op, int strategy, bool fusePrec);
+void prec_init_fp64(Context &c, int op);
+int  prec_invert(Context &c, int op);
+
+// helpers in context.cu
+int *status_ptr(Context &c);
+void read_status(Context &c, int *h, int n);
+
+}  // namespace mfem

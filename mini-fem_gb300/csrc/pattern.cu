@@ -1,0 +1,448 @@
+// CSR pattern and assembly plans, built on the device.
+//
+// Replaces the reference's host-side pattern code:
+//   create_nodeToNode  src/matrix.cc:55-91  (row pointers + 1-based columns in
+//                      first-occurrence order, from DC-lib's node->element lists)
+//   create_elemToEdge  src/matrix.cc:25-52  (16 CSR positions per element)
+// and adds the inverse map used by the owner-computes gather: for every CSR
+// entry, the (element, j, k) pairs that add to it, in ascending element order.
+//
+// Steps (all on the context stream):
+//   1. node -> element incidence: count, scan, fill, per-node sort (ascending
+//      element id, which is the order DC_create_nodeToElem lists them in);
+//   2. row pattern: one thread per row merges the nodes of its incident
+//      elements into a duplicate-free list (sorted, or in the reference's first
+//      occurrence order), count pass + scan + write pass;
+//   3. element -> 16 positions (binary search in sorted rows, linear otherwise);
+//   4. gather plan: one thread per row walks its incident elements in ascending
+//      order and appends (e, j, k) to the unit of entry (r, node_k) for every
+//      node_k >= r, so every unit list comes out ascending by construction.
+#include "context.h"
+
+namespace mfem {
+
+namespace {
+
+constexpr int kMaxRow = 128;   // longest row (distinct neighbours incl. self)
+constexpr int kThreads = 256;
+
+enum StatusBits { kRowOverflow = 1, kMissingEntry = 2, kBadIndex = 4 };
+
+__global__ void k_to_zero_based(const int *__restrict__ in, int *__restrict__ out,
+                                long long n, int nbNodes, int *status) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int v = in[i] - 1;
+    if (v < 0 || v >= nbNodes) {
+        atomicOr(status, kBadIndex);
+        v = 0;
+    }
+    out[i] = v;
+}
+
+__global__ void k_incidence_count(const int *__restrict__ e2n, long long n4, int *deg) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n4) atomicAdd(&deg[e2n[i]], 1);
+}
+
+__global__ void k_incidence_fill(const int *__restrict__ e2n, long long n4,
+                                 const int *__restrict__ ptr, int *fill, int *nodeElem) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n4) return;
+    int n = e2n[i];
+    int s = atomicAdd(&fill[n], 1);
+    nodeElem[ptr[n] + s] = (int)i;   // e*4 + j
+}
+
+__global__ void k_incidence_sort(const int *__restrict__ ptr, int *nodeElem, int nbNodes) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nbNodes) return;
+    int b = ptr[n], e = ptr[n + 1];
+    for (int i = b + 1; i < e; i++) {
+        int v = nodeElem[i];
+        int k = i - 1;
+        while (k >= b && nodeElem[k] > v) {
+            nodeElem[k + 1] = nodeElem[k];
+            k--;
+        }
+        nodeElem[k + 1] = v;
+    }
+}
+
+// Distinct neighbours of row r, in sorted or first-occurrence order.
+template <int ORDER>
+__device__ int row_neighbours(int r, const int *__restrict__ ptr,
+                              const int *__restrict__ nodeElem,
+                              const int *__restrict__ e2n, int *uniq, bool &overflow) {
+    int cnt = 0;
+    for (int p = ptr[r]; p < ptr[r + 1]; p++) {
+        int e = nodeElem[p] >> 2;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int c = e2n[4 * e + k];
+            if (ORDER == MFEM_ORDER_REFERENCE) {
+                bool found = false;
+                for (int m = 0; m < cnt; m++)
+                    if (uniq[m] == c) { found = true; break; }
+                if (!found) {
+                    if (cnt < kMaxRow) uniq[cnt++] = c;
+                    else overflow = true;
+                }
+            } else {
+                int m = cnt;
+                while (m > 0 && uniq[m - 1] > c) m--;
+                if (m > 0 && uniq[m - 1] == c) continue;
+                if (cnt >= kMaxRow) { overflow = true; continue; }
+                for (int q = cnt; q > m; q--) uniq[q] = uniq[q - 1];
+                uniq[m] = c;
+                cnt++;
+            }
+        }
+    }
+    return cnt;
+}
+
+template <int ORDER>
+__global__ void k_row_count(const int *__restrict__ ptr, const int *__restrict__ nodeElem,
+                            const int *__restrict__ e2n, int nbNodes, int *rowLen,
+                            int *status) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    int uniq[kMaxRow];
+    bool overflow = false;
+    int cnt = row_neighbours<ORDER>(r, ptr, nodeElem, e2n, uniq, overflow);
+    if (overflow) atomicOr(status, kRowOverflow);
+    rowLen[r] = cnt;
+}
+
+template <int ORDER>
+__global__ void k_row_write(const int *__restrict__ ptr, const int *__restrict__ nodeElem,
+                            const int *__restrict__ e2n, int nbNodes,
+                            const int *__restrict__ rowPtr, int *col, int *diagPos) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    int uniq[kMaxRow];
+    bool overflow = false;
+    int cnt = row_neighbours<ORDER>(r, ptr, nodeElem, e2n, uniq, overflow);
+    int base = rowPtr[r];
+    int dp = -1;
+    for (int m = 0; m < cnt; m++) {
+        col[base + m] = uniq[m];
+        if (uniq[m] == r) dp = base + m;
+    }
+    diagPos[r] = dp;
+}
+
+__device__ __forceinline__ int find_pos(const int *__restrict__ col, int b, int e, int c,
+                                        bool sorted) {
+    if (sorted) {
+        int lo = b, hi = e;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (col[mid] < c) lo = mid + 1; else hi = mid;
+        }
+        return (lo < e && col[lo] == c) ? lo : -1;
+    }
+    for (int p = b; p < e; p++)
+        if (col[p] == c) return p;
+    return -1;
+}
+
+__global__ void k_elem_pos(const int *__restrict__ e2n, long long n4,
+                           const int *__restrict__ rowPtr, const int *__restrict__ col,
+                           bool sorted, int *elemPos, int *status) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // e*4 + j
+    if (i >= n4) return;
+    long long e = i >> 2;
+    int r = e2n[i];
+    int b = rowPtr[r], en = rowPtr[r + 1];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        int p = find_pos(col, b, en, e2n[4 * e + k], sorted);
+        if (p < 0) atomicOr(status, kMissingEntry);
+        elemPos[i * 4 + k] = p < 0 ? 0 : p;
+    }
+}
+
+// Gather plan, pass A: number of contributions of every upper entry of row r.
+__global__ void k_plan_count(const int *__restrict__ ptr, const int *__restrict__ nodeElem,
+                             const int *__restrict__ e2n, const int *__restrict__ rowPtr,
+                             const int *__restrict__ col, bool sorted, int nbNodes,
+                             int *count, int *status) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    int b = rowPtr[r], en = rowPtr[r + 1];
+    for (int p = b; p < en; p++) count[p] = 0;
+    for (int q = ptr[r]; q < ptr[r + 1]; q++) {
+        int e = nodeElem[q] >> 2;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int c = e2n[4 * e + k];
+            if (c < r) continue;
+            int p = find_pos(col, b, en, c, sorted);
+            if (p < 0) { atomicOr(status, kMissingEntry); continue; }
+            count[p]++;
+        }
+    }
+}
+
+// Pass B: fill the lists (ascending element id since nodeElem is sorted) and
+// record the transposed position of every upper off-diagonal entry (entries of
+// a caller's pattern that no element touches get an empty list: value 0).
+__global__ void k_plan_fill(const int *__restrict__ ptr, const int *__restrict__ nodeElem,
+                            const int *__restrict__ e2n, const int *__restrict__ rowPtr,
+                            const int *__restrict__ col, bool sorted, int nbNodes,
+                            const int *__restrict__ start, int *fill, unsigned *contrib,
+                            int *tpos, int *status) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    int b = rowPtr[r], en = rowPtr[r + 1];
+    for (int p = b; p < en; p++) {
+        fill[p] = 0;
+        const int c = col[p];
+        if (c > r) {
+            // transposed entry (c, r); the pattern must be structurally symmetric
+            const int t = find_pos(col, rowPtr[c], rowPtr[c + 1], r, sorted);
+            if (t < 0) atomicOr(status, kMissingEntry);
+            tpos[p] = t < 0 ? p : t;
+        }
+    }
+    for (int q = ptr[r]; q < ptr[r + 1]; q++) {
+        int ej = nodeElem[q];
+        int e = ej >> 2, j = ej & 3;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int c = e2n[4 * e + k];
+            if (c < r) continue;
+            int p = find_pos(col, b, en, c, sorted);
+            if (p < 0) continue;
+            contrib[start[p] + fill[p]] = ((unsigned)e << 4) | ((unsigned)j << 2) | (unsigned)k;
+            fill[p]++;
+        }
+    }
+}
+
+// Off-diagonal upper units, bucketed by contribution count so that a warp
+// processes lists of equal length.
+__global__ void k_unit_hist(const int *__restrict__ rowOf, const int *__restrict__ col,
+                            const int *__restrict__ start, int nnz, int *hist) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nnz) return;
+    int r = rowOf[p];
+    if (col[p] <= r) return;
+    int n = start[p + 1] - start[p];
+    atomicAdd(&hist[min(n, 63)], 1);
+}
+
+__global__ void k_unit_place(const int *__restrict__ rowOf, const int *__restrict__ col,
+                             const int *__restrict__ start, const int *__restrict__ tpos,
+                             int nnz, int *bucketFill, int2 *unitPos) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nnz) return;
+    int r = rowOf[p];
+    if (col[p] <= r) return;
+    int n = start[p + 1] - start[p];
+    // descending count: bucket 63 first
+    int slot = atomicAdd(&bucketFill[63 - min(n, 63)], 1);
+    unitPos[slot] = make_int2(p, tpos[p]);
+}
+
+__global__ void k_row_of(const int *__restrict__ rowPtr, int nbNodes, int *rowOf) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    for (int p = rowPtr[r]; p < rowPtr[r + 1]; p++) rowOf[p] = r;
+}
+
+__global__ void k_reverse_hist_offsets(const int *hist, int *fill) {
+    // fill[b] = start of bucket (63 - b) in descending-count order
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int b = 0; b < 64; b++) {
+            fill[b] = s;
+            s += hist[63 - b];
+        }
+    }
+}
+
+void check_status(Context &c, const char *what) {
+    int st = 0;
+    read_status(c, &st, 1);
+    if (st & kBadIndex)
+        throw Error(MFEM_ERR_INVALID_ARG, std::string(what) + ": elemToNode index out of range");
+    if (st & kRowOverflow)
+        throw Error(MFEM_ERR_PATTERN, std::string(what) + ": a row has more than 128 entries");
+    if (st & kMissingEntry)
+        throw Error(MFEM_ERR_PATTERN, std::string(what) + ": pattern misses an element pair");
+}
+
+}  // namespace
+
+void build_incidence(Context &c) {
+    if (c.hasIncidence) return;
+    const long long n4 = 4LL * c.nbElem;
+    const int N = c.nbNodes;
+    int *ptr = (int *)c.nodeElemPtr.reserve(sizeof(int) * (N + 1));
+    int *deg = (int *)c.scratch.reserve(sizeof(int) * (size_t)(N + 1) * 2);
+    int *fill = deg + (N + 1);
+    int *tmp = (int *)c.scanTmp.reserve(sizeof(int) * scan_tmp_elems(N + 1));
+    MFEM_CUDA(cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)(N + 1) * 2, c.stream));
+    k_incidence_count<<<blocks_for(n4, kThreads), kThreads, 0, c.stream>>>(c.e2n.as<int>(), n4, deg);
+    check_launch("k_incidence_count");
+    exclusive_scan_i32(deg, ptr, N, tmp, c.stream);
+    int *ne = (int *)c.nodeElem.reserve(sizeof(int) * (size_t)n4);
+    k_incidence_fill<<<blocks_for(n4, kThreads), kThreads, 0, c.stream>>>(c.e2n.as<int>(), n4, ptr, fill, ne);
+    check_launch("k_incidence_fill");
+    k_incidence_sort<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, N);
+    check_launch("k_incidence_sort");
+    c.hasIncidence = true;
+}
+
+void build_pattern(Context &c, int order) {
+    MFEM_REQUIRE(order == MFEM_ORDER_SORTED || order == MFEM_ORDER_REFERENCE,
+                 MFEM_ERR_INVALID_ARG, "unknown column order");
+    build_incidence(c);
+    const int N = c.nbNodes;
+    int *st = status_ptr(c);
+    MFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(int), c.stream));
+    int *rowPtr = (int *)c.rowPtr.reserve(sizeof(int) * (N + 1));
+    int *tmp = (int *)c.scanTmp.reserve(sizeof(int) * scan_tmp_elems(N + 1));
+    const int *ptr = c.nodeElemPtr.as<int>(), *ne = c.nodeElem.as<int>(), *e2n = c.e2n.as<int>();
+    if (order == MFEM_ORDER_SORTED)
+        k_row_count<MFEM_ORDER_SORTED><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, st);
+    else
+        k_row_count<MFEM_ORDER_REFERENCE><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, st);
+    check_launch("k_row_count");
+    exclusive_scan_i32(rowPtr, rowPtr, N, tmp, c.stream);
+    int nnz = 0;
+    MFEM_CUDA(cudaMemcpyAsync(&nnz, rowPtr + N, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    MFEM_CUDA(cudaStreamSynchronize(c.stream));
+    check_status(c, "create_nodeToNode");
+    int *col = (int *)c.col.reserve(sizeof(int) * (size_t)nnz);
+    int *diag = (int *)c.diagPos.reserve(sizeof(int) * (size_t)N);
+    if (order == MFEM_ORDER_SORTED)
+        k_row_write<MFEM_ORDER_SORTED><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, col, diag);
+    else
+        k_row_write<MFEM_ORDER_REFERENCE><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, col, diag);
+    check_launch("k_row_write");
+    c.nnz = nnz;
+    c.order = order;
+    c.hasPattern = true;
+    c.hasElemPos = false;
+    c.gather.built = false;
+}
+
+__global__ void k_diag_from_pattern(const int *__restrict__ rowPtr, const int *__restrict__ col,
+                                    int nbNodes, int *diagPos) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    int dp = -1;
+    for (int p = rowPtr[r]; p < rowPtr[r + 1]; p++)
+        if (col[p] == r) { dp = p; break; }
+    diagPos[r] = dp;
+}
+
+__global__ void k_check_sorted(const int *__restrict__ rowPtr, const int *__restrict__ col,
+                               int nbNodes, int *notSorted) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    for (int p = rowPtr[r] + 1; p < rowPtr[r + 1]; p++)
+        if (col[p] <= col[p - 1]) { atomicOr(notSorted, 1); return; }
+}
+
+void adopt_pattern(Context &c, const int *hRow, const int *hCol, int nnz) {
+    const int N = c.nbNodes;
+    MFEM_REQUIRE(hRow[0] == 0 && hRow[N] == nnz, MFEM_ERR_PATTERN,
+                 "row pointers do not span nbEdges");
+    for (int i = 0; i < N; i++)
+        MFEM_REQUIRE(hRow[i + 1] >= hRow[i], MFEM_ERR_PATTERN, "row pointers decrease");
+    build_incidence(c);
+    int *rowPtr = (int *)c.rowPtr.reserve(sizeof(int) * (N + 1));
+    int *col = (int *)c.col.reserve(sizeof(int) * (size_t)nnz);
+    int *diag = (int *)c.diagPos.reserve(sizeof(int) * (size_t)N);
+    int *st = status_ptr(c);
+    MFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(int) * 2, c.stream));
+    MFEM_CUDA(cudaMemcpyAsync(rowPtr, hRow, sizeof(int) * (N + 1), cudaMemcpyHostToDevice, c.stream));
+    int *colIn = (int *)c.scratch.reserve(sizeof(int) * (size_t)nnz);
+    MFEM_CUDA(cudaMemcpyAsync(colIn, hCol, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, c.stream));
+    k_to_zero_based<<<blocks_for(nnz, kThreads), kThreads, 0, c.stream>>>(colIn, col, nnz, N, st);
+    check_launch("k_to_zero_based");
+    k_diag_from_pattern<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(rowPtr, col, N, diag);
+    check_launch("k_diag_from_pattern");
+    k_check_sorted<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(rowPtr, col, N, st + 1);
+    check_launch("k_check_sorted");
+    int h[2] = {0, 0};
+    read_status(c, h, 2);
+    MFEM_REQUIRE(!(h[0] & kBadIndex), MFEM_ERR_PATTERN, "column index out of range");
+    c.nnz = nnz;
+    c.order = h[1] ? MFEM_ORDER_REFERENCE : MFEM_ORDER_SORTED;   // unsorted: linear search
+    c.hasPattern = true;
+    c.hasElemPos = false;
+    c.gather.built = false;
+}
+
+void build_elem_pos(Context &c) {
+    MFEM_REQUIRE(c.hasPattern, MFEM_ERR_STATE, "no pattern");
+    if (c.hasElemPos) return;
+    const long long n4 = 4LL * c.nbElem;
+    int *ep = (int *)c.elemPos.reserve(sizeof(int) * (size_t)n4 * 4);
+    int *st = status_ptr(c);
+    MFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(int), c.stream));
+    k_elem_pos<<<blocks_for(n4, kThreads), kThreads, 0, c.stream>>>(
+        c.e2n.as<int>(), n4, c.rowPtr.as<int>(), c.col.as<int>(),
+        c.order == MFEM_ORDER_SORTED, ep, st);
+    check_launch("k_elem_pos");
+    check_status(c, "create_elemToEdge");
+    c.hasElemPos = true;
+}
+
+void build_gather_plan(Context &c) {
+    MFEM_REQUIRE(c.hasPattern, MFEM_ERR_STATE, "no pattern");
+    if (c.gather.built) return;
+    build_incidence(c);
+    const int N = c.nbNodes, nnz = c.nnz;
+    const bool sorted = c.order == MFEM_ORDER_SORTED;
+    GatherPlan &g = c.gather;
+    int *st = status_ptr(c);
+    MFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(int), c.stream));
+    // scratch layout: rowOf[nnz] | fill[nnz] | tpos[nnz] | hist[64] | bfill[64]
+    int *work = (int *)c.scratch2.reserve(sizeof(int) * ((size_t)nnz * 3 + 128));
+    int *rowOf = work, *fill = work + nnz, *tpos = work + 2LL * nnz;
+    int *hist = work + 3LL * nnz, *bfill = hist + 64;
+    int *start = (int *)g.unitStart.reserve(sizeof(int) * ((size_t)nnz + 1));
+    int *tmp = (int *)c.scanTmp.reserve(sizeof(int) * scan_tmp_elems(nnz + 1));
+    const int *ptr = c.nodeElemPtr.as<int>(), *ne = c.nodeElem.as<int>(), *e2n = c.e2n.as<int>();
+    const int *rowPtr = c.rowPtr.as<int>(), *col = c.col.as<int>();
+
+    k_plan_count<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, rowPtr, col, sorted, N, start, st);
+    check_launch("k_plan_count");
+    exclusive_scan_i32(start, start, nnz, tmp, c.stream);
+    int total = 0;
+    MFEM_CUDA(cudaMemcpyAsync(&total, start + nnz, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    MFEM_CUDA(cudaStreamSynchronize(c.stream));
+    check_status(c, "gather plan");
+    MFEM_REQUIRE(total == 10LL * c.nbElem, MFEM_ERR_PATTERN, "gather plan: contribution count mismatch");
+    unsigned *contrib = (unsigned *)g.contrib.reserve(sizeof(unsigned) * (size_t)total);
+    k_plan_fill<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, rowPtr, col, sorted, N, start, fill, contrib, tpos, st);
+    check_launch("k_plan_fill");
+    k_row_of<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(rowPtr, N, rowOf);
+    check_launch("k_row_of");
+    MFEM_CUDA(cudaMemsetAsync(hist, 0, sizeof(int) * 128, c.stream));
+    k_unit_hist<<<blocks_for(nnz, kThreads), kThreads, 0, c.stream>>>(rowOf, col, start, nnz, hist);
+    check_launch("k_unit_hist");
+    int hh[64];
+    MFEM_CUDA(cudaMemcpyAsync(hh, hist, sizeof(hh), cudaMemcpyDeviceToHost, c.stream));
+    MFEM_CUDA(cudaStreamSynchronize(c.stream));
+    int nEdge = 0;
+    for (int b = 0; b < 64; b++) nEdge += hh[b];
+    k_reverse_hist_offsets<<<1, 32, 0, c.stream>>>(hist, bfill);
+    int2 *upos = (int2 *)g.unitPos.reserve(sizeof(int2) * (size_t)(nEdge > 0 ? nEdge : 1));
+    k_unit_place<<<blocks_for(nnz, kThreads), kThreads, 0, c.stream>>>(rowOf, col, start, tpos, nnz, bfill, upos);
+    check_launch("k_unit_place");
+    check_status(c, "gather plan");
+    g.nUnits = nEdge;
+    g.nContrib = total;
+    g.nDiagUnits = N;
+    g.built = true;
+}
+
+}  // namespace mfem

@@ -1,0 +1,53 @@
+"""Full-size case of the benchmark (100^3 nodes, 5,821,794 tets): bit-exact FP64
+gather against the oracle on the whole matrix, and size-independent properties
+(symmetry, zero row sums of the Laplacian, idempotent re-assembly)."""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from minifem.meshgen import cube_mesh
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+
+@pytest.fixture(scope="module")
+def mesh():
+    return cube_mesh(100, seed=2024, op="ela")
+
+
+def test_fullsize_ela_fp64_bit_exact(gpu, mesh):
+    a = gpu(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("reference")
+    a.set_coefficients("ela", mesh.coef)
+    a.set_check_bounds(O.checkbounds(mesh.boundNodesCode))
+    a.assembly("ela", "fp64", "gather", prec=True)
+    v1 = a.values()
+    p1 = a.prec()
+    ref = O.full(mesh, op="ela")
+    assert np.array_equal(col, ref["col"])
+    assert v1.tobytes() == ref["values"].tobytes()
+    assert p1.tobytes() == ref["prec"].tobytes()
+    # re-assembly is idempotent (no state carried between iterations)
+    a.assembly("ela", "fp64", "gather", prec=True)
+    assert a.values().tobytes() == v1.tobytes()
+
+
+def test_fullsize_lap_symmetry_and_row_sums(gpu, mesh):
+    a = gpu(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    a.assembly("lap", "fp64", "gather")
+    v = a.values()
+    N = len(row) - 1
+    r = np.repeat(np.arange(N), np.diff(row))
+    # symmetric bit for bit: value(r, c) == value(c, r)
+    key = r.astype(np.int64) * N + (col - 1)
+    tkey = (col - 1).astype(np.int64) * N + r
+    order = np.argsort(key)
+    pos = order[np.searchsorted(key[order], tkey)]
+    assert np.array_equal(v, v[pos])
+    # gradients of the barycentric coordinates sum to zero: rows sum to ~0
+    rs = np.add.reduceat(v, row[:-1])
+    scale = np.add.reduceat(np.abs(v), row[:-1])
+    assert np.max(np.abs(rs) / scale) < 1e-12

@@ -1,0 +1,252 @@
+"""GPU path against the oracle: bit-exact for the FP64 gather (the reference's
+summation order, -fmad=false), the pattern, positions and the preconditioner;
+within stated tolerances for the colour scatter, the atomic strategy and FP32."""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from conftest import golden_cases, load_golden
+from minifem.meshgen import cube_mesh
+
+pytestmark = pytest.mark.gpu
+
+# FP64 strategies other than the ordered gather: error per entry relative to
+# the sum of magnitudes of that entry's contributions (hard cancellation makes a
+# plain relative error meaningless for near-zero entries).
+TOL_FP64_REORDERED = 1e-13
+# FP32 (compensated sums, FP64 slivers): error relative to the block scale
+# sum_e |g_j| |g_k| max(A, B, mu) of the entry's contributions.
+TOL_FP32 = 1e-6
+
+
+def keyed(row, col, vals, dim):
+    """{(r, c): block} dictionary-free form: sort entries by (row, col)."""
+    N = len(row) - 1
+    r = np.repeat(np.arange(N), np.diff(row))
+    order = np.lexsort((col, r))
+    return r[order], col[order], vals.reshape(-1, dim)[order]
+
+
+def contribution_scale(mesh, row, col, op, coef):
+    """Per-entry sum of |contribution| magnitudes (FP64), keyed like `keyed`."""
+    e2e = O.elem_to_edge(row, col, mesh.elemToNode).reshape(-1, 16)
+    X = mesh.coord[mesh.elemToNode - 1]
+    a, b, c = X[:, 0] - X[:, 3], X[:, 2] - X[:, 3], X[:, 1] - X[:, 3]
+    G = np.empty((len(a), 4, 3))
+    G[:, 0] = np.cross(b, c); G[:, 1] = np.cross(c, a); G[:, 2] = np.cross(a, b)
+    G[:, 3] = -(G[:, 0] + G[:, 1] + G[:, 2])
+    vol = np.einsum("ij,ij->i", a, G[:, 0])
+    G /= vol[:, None, None]
+    gn = np.linalg.norm(G, axis=2)
+    if coef is None:
+        w = np.full(len(a), 2.25 if op == "ela" else 1.0)
+    elif op == "lap":
+        w = coef
+    else:
+        E, nu = coef[:, 0], coef[:, 1]
+        lam = E * nu / ((1 + nu) * (1 - 2 * nu)); mu = E / (2 * (1 + nu))
+        w = lam + 2 * mu
+    sc = (gn[:, :, None] * gn[:, None, :] * w[:, None, None]).reshape(-1)
+    S = np.zeros(len(col)); np.add.at(S, e2e.reshape(-1), sc)
+    return S
+
+
+def gpu_full(Asm, mesh, op, coef, order="reference", precision="fp64", strategy="gather",
+             fused=False):
+    a = Asm(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode(order)
+    a.set_coefficients(op, coef)
+    a.set_check_bounds(O.checkbounds(mesh.boundNodesCode))
+    if strategy == "scatter":
+        a.coloring_creation(seed=1)
+    if fused:
+        a.assembly(op, precision, strategy, prec=True)
+    else:
+        a.assembly(op, precision, strategy)
+        a.prec_init()
+        a.prec_inversion()
+    vals = a.values()
+    prec = a.prec()
+    a.close()
+    return row, col, vals, prec
+
+
+@pytest.mark.parametrize("name", golden_cases())
+@pytest.mark.parametrize("fused", [False, True])
+def test_gather_fp64_bit_exact_vs_golden(gpu, name, fused):
+    g = load_golden(name)
+    op = str(g["op"])
+
+    class M:  # golden fixture as a mesh
+        coord, elemToNode, boundNodesCode = g["coord"], g["elemToNode"], g["boundNodesCode"]
+    row, col, vals, prec = gpu_full(gpu, M, op, None, "reference", fused=fused)
+    assert np.array_equal(row, g["row"]) and np.array_equal(col, g["col"])
+    assert vals.tobytes() == g["values"].tobytes()
+    assert prec.tobytes() == g["prec"].tobytes()
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_colour_ordered_golden_bit_exact(gpu, name):
+    """The COLORING build's result (colour-permuted elements) is reproduced bit for
+    bit by the gather on the permuted mesh: ascending element order is exactly
+    its visiting order."""
+    g = load_golden(name)
+    op = str(g["op"])
+    a = gpu(0)
+    a.set_mesh(g["coord"], g["color_elemToNode"])
+    row, col = a.create_nodeToNode("reference")
+    assert np.array_equal(col, g["color_col"])
+    a.assembly(op)
+    assert a.values().tobytes() == g["color_values"].tobytes()
+
+
+@pytest.mark.parametrize("n,op,seed,coef,jit", [
+    (6, "lap", 1, False, 0.2), (6, "ela", 2, False, 0.2), (9, "lap", 3, True, 0.2),
+    (9, "ela", 4, True, 0.2), (11, "ela", 5, True, 0.45), (14, "lap", 6, True, 0.2),
+    (14, "ela", 7, True, 0.2)])
+@pytest.mark.parametrize("order", ["sorted", "reference"])
+def test_gather_fp64_bit_exact_vs_oracle(gpu, n, op, seed, coef, jit, order):
+    m = cube_mesh(n, seed=seed, op=op, jitter=jit)
+    c = m.coef if coef else None
+    row, col, vals, prec = gpu_full(gpu, m, op, c, order)
+    ref = O.full(m, op=op, coef=c)
+    if order == "reference":
+        assert np.array_equal(row, ref["row"]) and np.array_equal(col, ref["col"])
+        assert vals.tobytes() == ref["values"].tobytes()
+    else:
+        # same entries, ascending columns
+        d = O.op_dim(op)
+        r1, c1, v1 = keyed(row, col, vals, d)
+        r2, c2, v2 = keyed(ref["row"], ref["col"], ref["values"], d)
+        assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+        assert v1.tobytes() == v2.tobytes()
+    assert prec.tobytes() == ref["prec"].tobytes()
+
+
+def test_elem_to_edge_matches_reference(gpu):
+    m = cube_mesh(8, seed=3)
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    row, col = a.create_nodeToNode("reference")
+    assert np.array_equal(a.create_elemToEdge(), O.elem_to_edge(row, col, m.elemToNode))
+
+
+@pytest.mark.parametrize("strategy", ["scatter", "atomic"])
+@pytest.mark.parametrize("op", ["lap", "ela"])
+def test_reordered_fp64_strategies(gpu, strategy, op):
+    m = cube_mesh(12, seed=8, op=op)
+    row, col, vals, prec = gpu_full(gpu, m, op, m.coef, "reference", strategy=strategy)
+    ref = O.full(m, op=op)
+    d = O.op_dim(op)
+    S = contribution_scale(m, ref["row"], ref["col"], op, m.coef)
+    err = np.abs(vals.reshape(-1, d) - ref["values"].reshape(-1, d)) / S[:, None]
+    assert err.max() < TOL_FP64_REORDERED
+
+
+def test_colouring_is_valid(gpu):
+    m = cube_mesh(10, seed=2)
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    perm, index = a.coloring_creation(seed=5)
+    E = m.nbElem
+    assert sorted(perm) == list(range(E))
+    assert index[0] == 0 and index[-1] == E and len(index) - 1 <= 128
+    colour = np.searchsorted(index, perm, side="right") - 1
+    # no two elements sharing a node carry the same colour
+    for k in range(4):
+        for l in range(k + 1, 4):
+            pass
+    node_col = {}
+    for e in range(E):
+        for nd in m.elemToNode[e]:
+            key = (int(nd), int(colour[e]))
+            assert key not in node_col, "colour conflict"
+            node_col[key] = e
+    # stable within a colour
+    for c in range(len(index) - 1):
+        members = np.nonzero(colour == c)[0]
+        assert np.all(np.diff(perm[members]) == 1)
+
+
+@pytest.mark.parametrize("op,n,jit,sliver", [("lap", 14, 0.2, 0.0), ("ela", 14, 0.2, 0.0),
+                                              ("ela", 12, 0.45, 0.05)])
+def test_fp32_within_tolerance(gpu, op, n, jit, sliver):
+    m = cube_mesh(n, seed=11, op=op, jitter=jit, sliver_fraction=sliver,
+                  jump=1e6 if sliver else 1.0, nu_max=0.45 if sliver else 0.35)
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    row, col = a.create_nodeToNode("reference")
+    a.set_coefficients(op, m.coef)
+    a.set_check_bounds(O.checkbounds(m.boundNodesCode))
+    a.assembly(op, "fp32", "gather", prec=True)
+    v32 = a.values_f32().astype(np.float64)
+    ref = O.full(m, op=op)
+    d = O.op_dim(op)
+    S = contribution_scale(m, ref["row"], ref["col"], op, m.coef)
+    err = np.abs(v32.reshape(-1, d) - ref["values"].reshape(-1, d)) / S[:, None]
+    assert err.max() < TOL_FP32, err.max()
+    if sliver:
+        assert a.flagged() > 0
+
+
+def test_reference_shaped_calls_bit_exact(gpu):
+    """assembly / prec_init / prec_inversion with the reference's arguments."""
+    import minifem
+    m = cube_mesh(8, seed=4, op="ela")
+    ref = O.full(m, op="ela", coef=None)
+    row, col = ref["row"], ref["col"]
+    nnz = int(row[-1])
+    a = gpu(0)
+    vals = np.zeros(nnz * 9)
+    e2n = np.ascontiguousarray(m.elemToNode.reshape(-1))
+    for _ in range(2):   # second call reuses the cached pattern
+        minifem.assembly(m.coord, vals, row, col, e2n, None, m.nbElem, nnz, 9, 1, ctx=a)
+        assert vals.tobytes() == ref["values"].tobytes()
+        prec = np.zeros(m.nbNodes * 9)
+        minifem.prec_init(prec, vals, row, col, m.nbNodes, 9, ctx=a)
+        minifem.prec_inversion(prec, row, col, ref["checkBounds"], m.nbNodes, 1, ctx=a)
+        assert prec.tobytes() == ref["prec"].tobytes()
+
+
+def test_errors_are_reported_not_faulted(gpu):
+    import minifem
+    m = cube_mesh(4, seed=1)
+    a = gpu(0)
+    with pytest.raises(minifem.MfemError):          # assembly before any mesh
+        a.assembly("ela")
+    bad = m.elemToNode.copy()
+    bad[0, 0] = m.nbNodes + 5
+    with pytest.raises(minifem.MfemError):          # node index out of range
+        a.set_mesh(m.coord, bad)
+    a.set_mesh(m.coord, m.elemToNode)
+    with pytest.raises(minifem.MfemError):          # pattern missing
+        a.assembly("ela")
+    row, col = a.create_nodeToNode()
+    # a pattern that misses an element pair is rejected
+    r2, c2 = row.copy(), col.copy()
+    c2[1] = c2[0]
+    with pytest.raises(minifem.MfemError):
+        a.set_pattern(r2, c2)
+    with pytest.raises(minifem.MfemError):          # scatter without colouring
+        b = gpu(0)
+        b.set_mesh(m.coord, m.elemToNode)
+        b.create_nodeToNode()
+        b.assembly("ela", "fp64", "scatter")
+
+
+def test_isolated_node_and_singular_block(gpu):
+    """A node no element touches: prec_init leaves zeros, the lap inverse is inf
+    and the ela block (no diagonal entry) is left as masked (elasclpr.f:29-32)."""
+    m = cube_mesh(3, seed=1, op="lap", coefficients=False)
+    coord = np.vstack([m.coord, [[5.0, 5.0, 5.0]]])
+    code = np.concatenate([m.boundNodesCode, [0]]).astype(np.int32)
+
+    class M:
+        pass
+    M.coord, M.elemToNode, M.boundNodesCode = coord, m.elemToNode, code
+    for op in ("lap", "ela"):
+        row, col, vals, prec = gpu_full(gpu, M, op, None, "reference")
+        ref = O.full(M, op=op, coef=None)
+        assert vals.tobytes() == ref["values"].tobytes()
+        assert prec.tobytes() == ref["prec"].tobytes()
