@@ -117,7 +117,7 @@ int mfem_assemble_prec(mfem_context *ctx, int operatorID, int precision, int str
 
 /* FP32 precision: elements whose shape quality |6V| / (|a| |b| |c|) (a, b, c the
  * edge vectors from the fourth node) is below `threshold` are integrated in FP64
- * (default 0.05).  *nbFlagged receives the count of the last FP32 assembly. */
+ * (default 0.1).  *nbFlagged receives the count of the last FP32 assembly. */
 int mfem_set_sliver_threshold(mfem_context *ctx, double threshold);
 int mfem_get_flagged(mfem_context *ctx, int *nbFlagged);
 

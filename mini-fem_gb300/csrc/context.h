@@ -89,7 +89,7 @@ struct Context {
     // FP32 path: elements whose quality |6V| / (|a||b||c|) is below this
     // threshold get their Jacobian in FP64; the count of the last assembly is
     // kept in status[5].
-    float sliverThreshold = 0.05f;
+    float sliverThreshold = 0.1f;
     bool flaggedPending = false;
 
     // scratch

@@ -33,7 +33,8 @@ def contribution_scale(mesh, row, col, op, coef):
     X = mesh.coord[mesh.elemToNode - 1]
     a, b, c = X[:, 0] - X[:, 3], X[:, 2] - X[:, 3], X[:, 1] - X[:, 3]
     G = np.empty((len(a), 4, 3))
-    G[:, 0] = np.cross(b, c); G[:, 1] = np.cross(c, a); G[:, 2] = np.cross(a, b)
+    # rows as assembly.cc:106-114 forms them: g0 = b x c, g1 = a x b, g2 = c x a
+    G[:, 0] = np.cross(b, c); G[:, 1] = np.cross(a, b); G[:, 2] = np.cross(c, a)
     G[:, 3] = -(G[:, 0] + G[:, 1] + G[:, 2])
     vol = np.einsum("ij,ij->i", a, G[:, 0])
     G /= vol[:, None, None]
@@ -245,6 +246,7 @@ def test_isolated_node_and_singular_block(gpu):
     class M:
         pass
     M.coord, M.elemToNode, M.boundNodesCode = coord, m.elemToNode, code
+    M.nbNodes, M.nbElem = coord.shape[0], m.nbElem
     for op in ("lap", "ela"):
         row, col, vals, prec = gpu_full(gpu, M, op, None, "reference")
         ref = O.full(M, op=op, coef=None)
