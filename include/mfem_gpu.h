@@ -65,7 +65,9 @@ int mfem_get_stream(mfem_context *ctx, void **stream);
 
 /* ---- mesh (src/IO.cc:61-96 arrays) ----------------------------------------- */
 /* Uploads coord[nbNodes*3] and elemToNode[nbElem*4] (1-based).  Replaces the
- * mesh and drops every structure built on the previous one. */
+ * mesh and drops every structure built on the previous one.  coord may be NULL
+ * (topology only, as create_nodeToNode sees the mesh); assembly then needs
+ * mfem_update_coords first. */
 int mfem_set_mesh(mfem_context *ctx, const double *coord, const int *elemToNode,
                   int nbElem, int nbNodes);
 /* New coordinates for the same topology (keeps pattern, colouring, plans). */

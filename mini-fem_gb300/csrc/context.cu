@@ -94,7 +94,7 @@ void require_pattern(Context &c) {
 }
 
 void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int nbNodes) {
-    MFEM_REQUIRE(coord && e2n, MFEM_ERR_INVALID_ARG, "null mesh array");
+    MFEM_REQUIRE(e2n, MFEM_ERR_INVALID_ARG, "null elemToNode");
     MFEM_REQUIRE(nbElem > 0 && nbNodes > 0, MFEM_ERR_INVALID_ARG, "empty mesh");
     MFEM_REQUIRE((long long)nbElem * 10 < (1LL << 31) && nbElem < (1 << 27),
                  MFEM_ERR_CAPACITY, "mesh too large for 32-bit plan indices");
@@ -108,8 +108,10 @@ void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int n
     c.lastOp = -1;
     c.hostRow = c.hostCol = nullptr;
     double *dc = (double *)c.coord.reserve(sizeof(double) * 3 * (size_t)nbNodes);
-    MFEM_CUDA(cudaMemcpyAsync(dc, coord, sizeof(double) * 3 * (size_t)nbNodes,
-                              cudaMemcpyHostToDevice, c.stream));
+    c.hasCoords = coord != nullptr;   // topology-only meshes get coordinates later
+    if (coord)
+        MFEM_CUDA(cudaMemcpyAsync(dc, coord, sizeof(double) * 3 * (size_t)nbNodes,
+                                  cudaMemcpyHostToDevice, c.stream));
     const long long n4 = 4LL * nbElem;
     int *raw = (int *)c.scratch.reserve(sizeof(int) * (size_t)n4);
     int *de = (int *)c.e2n.reserve(sizeof(int) * (size_t)n4);
@@ -131,6 +133,7 @@ void upload_coords(Context &c, const double *coord) {
     MFEM_REQUIRE(coord, MFEM_ERR_INVALID_ARG, "null coord");
     MFEM_CUDA(cudaMemcpyAsync(c.coord.as<double>(), coord, sizeof(double) * 3 * (size_t)c.nbNodes,
                               cudaMemcpyHostToDevice, c.stream));
+    c.hasCoords = true;
 }
 
 void download_col(Context &c, int *col) {
@@ -142,6 +145,7 @@ void download_col(Context &c, int *col) {
 
 void assemble(Context &c, int op, int precision, int strategy, bool fusePrec) {
     require_pattern(c);
+    MFEM_REQUIRE(c.hasCoords, MFEM_ERR_STATE, "no coordinates (mfem_update_coords first)");
     MFEM_REQUIRE(op == MFEM_OP_LAP || op == MFEM_OP_ELA, MFEM_ERR_INVALID_ARG, "operatorID must be 0 or 1");
     MFEM_REQUIRE(precision == MFEM_FP64 || precision == MFEM_FP32, MFEM_ERR_INVALID_ARG, "unknown precision");
     if (strategy == MFEM_AUTO) strategy = MFEM_GATHER;

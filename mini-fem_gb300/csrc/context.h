@@ -55,6 +55,7 @@ struct Context {
 
     // mesh
     int nbElem = 0, nbNodes = 0;
+    bool hasCoords = false;
     DevBuf coord;      // double [N*3]
     DevBuf e2n;        // int    [E*4], 0-based
     const void *hostE2n = nullptr;   // identity of the caller's elemToNode
