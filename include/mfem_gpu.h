@@ -143,6 +143,28 @@ int mfem_profile_read(mfem_context *ctx, char *names, int namesCap, float *ms, i
 int mfem_get_sizes(mfem_context *ctx, int *nbElem, int *nbNodes, int *nbEdges,
                    int *nbColors);
 
+/* ---- allocation-free assembly ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they assemble -- code recorded into a CUDA graph by stream
+ * capture, solvers whose device memory belongs to their own pool allocator,
+ * real-time loops that must not risk an allocation failure -- this runs the
+ * FP64 gather (the kernels and results of mfem_assemble with MFEM_FP64 and
+ * MFEM_GATHER, without the preconditioner) and calls no cudaMalloc, cudaFree or
+ * allocating library routine.  coord (nbNodes*3), coef (as
+ * mfem_set_coefficients, or NULL for the reference constants) and values
+ * (nbEdges*opDim) are DEVICE pointers the caller owns; topology and gather plan
+ * are the context's (mfem_assemble with MFEM_FP64/MFEM_GATHER must have run once).
+ * Its scratch is one fixed array inside the library of at most 131072 elements
+ * (16 MiB of gradient records), held by every GPU that loads the library until
+ * the process exits; larger meshes get MFEM_ERR_CAPACITY.  The first call on a
+ * device looks the array's device address up (and may load the module holding
+ * it), so make that first call before any stream capture.  Work is enqueued on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) without waiting.
+ * All calls share the one array and every call overwrites it: calls that overlap
+ * on the GPU (e.g. on two streams) race and must be serialised by the caller. */
+int mfem_assemble_noalloc(mfem_context *ctx, int operatorID, const double *coord,
+                          const double *coef, double *values, void *stream);
+
 /* ---- reference-shaped single calls (host buffers in and out) ---------------- */
 /* Same arguments and meaning as the reference operators; each call uploads what
  * it reads and downloads what it writes.  nodeToNodeRow / nodeToNodeColumn must

@@ -371,6 +371,46 @@ void assemble_fp64(Context &c, int op, int strategy, bool fusePrec) {
     c.precIsInit = fusePrec && strategy == MFEM_GATHER;
 }
 
+// FP64 gather on caller-provided buffers: coordinates, coefficients (NULL: the
+// reference constants), gradient-record scratch (16 doubles per element) and
+// values.  Uses the context's topology and gather plan, which must exist;
+// launches on `s` and allocates nothing.
+void gather_fp64_into(const Context &c, int op, const double *coord, const double *coef,
+                      double *rec, double *values, cudaStream_t s) {
+    const GatherPlan &g = c.gather;
+    const int E = c.nbElem, N = c.nbNodes;
+    const int *dp = c.diagPos.as<int>(), *st = g.unitStart.as<int>();
+    const unsigned *ct = g.contrib.as<unsigned>();
+    const int2 *up = g.unitPos.as<int2>();
+    const int4 *e2n = c.e2n.as<int4>();
+    if (op == MFEM_OP_LAP) {
+        if (coef) {
+            k_grad64<MFEM_OP_LAP, true><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
+            k_diag_units64<MFEM_OP_LAP, true, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            if (g.nUnits > 0)
+                k_edge_units64<MFEM_OP_LAP, true><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
+        } else {
+            k_grad64<MFEM_OP_LAP, false><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, nullptr, E, rec);
+            k_diag_units64<MFEM_OP_LAP, false, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            if (g.nUnits > 0)
+                k_edge_units64<MFEM_OP_LAP, false><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
+        }
+    } else {
+        if (coef) {
+            k_grad64<MFEM_OP_ELA, true><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
+            k_diag_units64<MFEM_OP_ELA, true, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            if (g.nUnits > 0)
+                k_edge_units64<MFEM_OP_ELA, true><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
+        } else {
+            k_grad64<MFEM_OP_ELA, false><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, nullptr, E, rec);
+            k_diag_units64<MFEM_OP_ELA, false, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            if (g.nUnits > 0)
+                k_edge_units64<MFEM_OP_ELA, false><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
+        }
+    }
+    check_launch("gather_fp64_into");
+}
+
 void prec_init_fp64(Context &c, int op) {
     const int dim = op == MFEM_OP_LAP ? 1 : 9;
     double *prec = (double *)c.prec.reserve(sizeof(double) * (size_t)c.nbNodes * dim);

@@ -8,10 +8,6 @@
 
 #include "context.h"
 
-struct mfem_context {
-    mfem::Context c;
-};
-
 namespace mfem {
 
 int *status_ptr(Context &c) { return c.status.as<int>(); }

@@ -119,3 +119,8 @@ int *status_ptr(Context &c);
 void read_status(Context &c, int *h, int n);
 
 }  // namespace mfem
+
+// The opaque handle of the C ABI.
+struct mfem_context {
+    mfem::Context c;
+};

@@ -53,6 +53,7 @@ _SIGS = {
     "mfem_profile": ([_vp, C.c_int], C.c_int),
     "mfem_profile_read": ([_vp, C.c_char_p, C.c_int, _fp, C.c_int, _ip], C.c_int),
     "mfem_get_sizes": ([_vp, _ip, _ip, _ip, _ip], C.c_int),
+    "mfem_assemble_noalloc": ([_vp, C.c_int, _vp, _vp, _vp, _vp], C.c_int),
     "mfem_assembly": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int],
                       C.c_int),
     "mfem_prec_init_host": ([_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int], C.c_int),
