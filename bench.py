@@ -128,6 +128,9 @@ def kernel_bytes(name, E, N, nnz, n_edge_units, fp32):
         if "prec" in name:
             b += N * 9 * 8 + N
         return b
+    if name.startswith("tile32"):
+        # the tile kernel is the whole step but the coordinate split: the step's bytes
+        return step_bytes(E, N, nnz, fp32)
     if name.startswith("grad"):
         coordb = 32 * N if fp32 else 24 * N
         return 16 * E + coordb + (8 if fp32 else 16) * E + rec * E
@@ -274,8 +277,8 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": None,
         "clocks": clk.summary(),
     }
-    # own kernels launched per timed step (fp32 step: split, coef, grad, diag, edge)
-    out["gpu_launches"] = 5 * args.steps
+    # own kernels launched per timed step (fp32 step, tile kernel: split + tile)
+    out["gpu_launches"] = len(prof["fp32"]) * args.steps
     if args.cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(mesh, row, col, markf, args.cpu_iters)
     a.close()

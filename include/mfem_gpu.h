@@ -122,6 +122,11 @@ int mfem_assemble_prec(mfem_context *ctx, int operatorID, int precision, int str
  * (default 0.1).  *nbFlagged receives the count of the last FP32 assembly. */
 int mfem_set_sliver_threshold(mfem_context *ctx, double threshold);
 int mfem_get_flagged(mfem_context *ctx, int *nbFlagged);
+/* Tuning knobs (no counterpart in the reference): "sliver_threshold" (as above),
+ * "fp32_kernel" (0: per-element gradient records + one thread per entry,
+ * 1: spatial row tiles with gradients in shared memory, the default),
+ * "tile_rows" / "tile_elems" (tile size limits of kernel 1). */
+int mfem_set_option(mfem_context *ctx, const char *name, double value);
 
 /* ---- results ---------------------------------------------------------------- */
 int mfem_get_values(mfem_context *ctx, double *values);     /* nbEdges*opDim, FP64 */

@@ -98,6 +98,7 @@ void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int n
     c.nbNodes = nbNodes;
     c.hasPattern = c.hasIncidence = c.hasElemPos = false;
     c.gather.built = false;
+    c.tiles.built = false;
     c.coloring.built = false;
     c.coefOp = -1;
     c.hasMask = false;
@@ -385,6 +386,30 @@ int mfem_set_sliver_threshold(mfem_context *ctx, double threshold) {
         MFEM_REQUIRE(threshold >= 0.0 && threshold <= 1.0, MFEM_ERR_INVALID_ARG,
                      "threshold must lie in [0, 1]");
         c.sliverThreshold = (float)threshold;
+    });
+}
+
+int mfem_set_option(mfem_context *ctx, const char *name, double value) {
+    return mfem::guarded(ctx, [&](Context &c) {
+        MFEM_REQUIRE(name, MFEM_ERR_INVALID_ARG, "null option name");
+        const std::string n(name);
+        if (n == "sliver_threshold") {
+            MFEM_REQUIRE(value >= 0.0 && value <= 1.0, MFEM_ERR_INVALID_ARG, "threshold must lie in [0, 1]");
+            c.sliverThreshold = (float)value;
+        } else if (n == "fp32_kernel") {
+            MFEM_REQUIRE(value == 0.0 || value == 1.0, MFEM_ERR_INVALID_ARG, "fp32_kernel is 0 or 1");
+            c.fp32Kernel = (int)value;
+        } else if (n == "tile_rows") {
+            MFEM_REQUIRE(value >= 1 && value <= 1024, MFEM_ERR_INVALID_ARG, "tile_rows in [1, 1024]");
+            c.tiles.maxRows = (int)value;
+            c.tiles.built = false;
+        } else if (n == "tile_elems") {
+            MFEM_REQUIRE(value >= 64 && value <= 4096, MFEM_ERR_INVALID_ARG, "tile_elems in [64, 4096]");
+            c.tiles.maxElem = (int)value;
+            c.tiles.built = false;
+        } else {
+            throw Error(MFEM_ERR_INVALID_ARG, "unknown option " + n);
+        }
     });
 }
 

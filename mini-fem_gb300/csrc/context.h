@@ -26,6 +26,16 @@ struct GatherPlan {
     DevBuf diagNode;    // int [nDiagUnits]  node of each diagonal unit
 };
 
+// FP32 spatial-tile plan (tiles.cu): rows in Morton order cut into tiles of at
+// most maxRows rows touching at most maxElem elements.
+struct TilePlan {
+    bool built = false;
+    int maxRows = 64, maxElem = 640;
+    int nTiles = 0;
+    long long nTileElems = 0;   // sum over tiles of their element counts
+    DevBuf desc, rows, elems, offPos, offMeta, diagMeta, contrib;
+};
+
 struct Coloring {
     bool built = false;
     int nbColors = 0;
@@ -71,7 +81,9 @@ struct Context {
     const void *hostRow = nullptr, *hostCol = nullptr;  // identity of caller's CSR
 
     GatherPlan gather;
+    TilePlan tiles;
     Coloring coloring;
+    int fp32Kernel = 1;               // 0: gradient records + unit gather, 1: tiles
 
     // coefficients
     int coefOp = -1;                  // -1: reference constants
@@ -105,6 +117,10 @@ void build_pattern(Context &c, int order);
 void adopt_pattern(Context &c, const int *hRow, const int *hCol, int nnz);
 void build_elem_pos(Context &c);
 void build_gather_plan(Context &c);
+
+// tiles.cu
+void build_tile_plan(Context &c);
+void assemble_tiles32(Context &c, int op, bool fusePrec);
 
 // coloring.cu
 void build_coloring(Context &c, unsigned long long seed);

@@ -1,0 +1,106 @@
+// Per-element arithmetic of the FP32 path (shared by the record kernel and the
+// tile kernel).  Coordinates arrive split into float hi + lo parts so that the
+// edge vectors are the FP64 differences rounded once to FP32; cross products use
+// Kahan's a*b - c*d with an FMA; elements below the quality threshold get their
+// gradients from the FP64 formula (elem_math.cuh) instead.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "elem_math.cuh"
+
+namespace mfem {
+
+// a*b - c*d with one rounding error less than the plain expression (Kahan).
+__device__ __forceinline__ float diff_prod(float a, float b, float c, float d) {
+    const float w = c * d;
+    const float e = fmaf(-c, d, w);
+    const float f = fmaf(a, b, -w);
+    return f + e;
+}
+
+// Gradients g[4][3] of one element in FP32.  Returns true when the element was
+// flagged (quality |6V| / (|a||b||c|) below sqrt(qthr2)) and computed in FP64.
+__device__ __forceinline__ bool grad32(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                       const double *__restrict__ coord, int4 nd, float qthr2,
+                                       float g[12]) {
+    const float4 h0 = hi[nd.x], h1 = hi[nd.y], h2 = hi[nd.z], h3 = hi[nd.w];
+    const float4 l0 = lo[nd.x], l1 = lo[nd.y], l2 = lo[nd.z], l3 = lo[nd.w];
+    const float xa = (h0.x - h3.x) + (l0.x - l3.x), ya = (h0.y - h3.y) + (l0.y - l3.y),
+                za = (h0.z - h3.z) + (l0.z - l3.z);
+    const float xb = (h2.x - h3.x) + (l2.x - l3.x), yb = (h2.y - h3.y) + (l2.y - l3.y),
+                zb = (h2.z - h3.z) + (l2.z - l3.z);
+    const float xc = (h1.x - h3.x) + (l1.x - l3.x), yc = (h1.y - h3.y) + (l1.y - l3.y),
+                zc = (h1.z - h3.z) + (l1.z - l3.z);
+    g[0] = diff_prod(yb, zc, yc, zb); g[1] = diff_prod(zb, xc, zc, xb); g[2] = diff_prod(xb, yc, xc, yb);
+    g[3] = diff_prod(ya, zb, yb, za); g[4] = diff_prod(za, xb, zb, xa); g[5] = diff_prod(xa, yb, xb, ya);
+    g[6] = diff_prod(yc, za, ya, zc); g[7] = diff_prod(zc, xa, za, xc); g[8] = diff_prod(xc, ya, xa, yc);
+    const float vol = fmaf(xa, g[0], fmaf(ya, g[1], za * g[2]));
+    const float na = fmaf(xa, xa, fmaf(ya, ya, za * za));
+    const float nb = fmaf(xb, xb, fmaf(yb, yb, zb * zb));
+    const float nc = fmaf(xc, xc, fmaf(yc, yc, zc * zc));
+    if (vol * vol < qthr2 * (na * nb) * nc) {
+        double gd[12];
+        elem_gradients(coord, nd, gd);
+#pragma unroll
+        for (int i = 0; i < 12; i++) g[i] = __double2float_rn(gd[i]);
+        return true;
+    }
+    g[9] = -((g[0] + g[3]) + g[6]);
+    g[10] = -((g[1] + g[4]) + g[7]);
+    g[11] = -((g[2] + g[5]) + g[8]);
+    const float r = 1.0f / vol;
+#pragma unroll
+    for (int i = 0; i < 12; i++) g[i] *= r;
+    return false;
+}
+
+// Weights (A, B, mu) of the elasticity blocks, or (kappa, -, -) for lap, in FP32
+// from the FP64 per-element coefficients (NULL: the reference constants).
+template <int OP>
+__device__ __forceinline__ float4 weights32(const double *__restrict__ coef, int e) {
+    if (OP == MFEM_OP_LAP) return make_float4(coef ? __double2float_rn(coef[e]) : 1.0f, 0.f, 0.f, 0.f);
+    if (!coef) return make_float4(2.25f, 1.25f, 1.0f, 0.f);
+    const double2 c = reinterpret_cast<const double2 *>(coef)[e];
+    const float E = __double2float_rn(c.x), nu = __double2float_rn(c.y);
+    const float lam = (E * nu) / ((1.0f + nu) * (1.0f - 2.0f * nu));
+    const float mu = E / (2.0f * (1.0f + nu));
+    return make_float4(fmaf(2.0f, mu, lam), lam + mu, mu, 0.f);
+}
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s - c; }
+};
+
+// Inverse of a symmetric-positive 3x3 block (column-major, FP64) by cofactors
+// with FMAs; returns false when the determinant is exactly zero (block left as
+// it is).  Used by the FP32 path, whose preconditioner is not tied to the
+// reference's LAPACK operation order.
+__device__ __forceinline__ bool inv3_cofactor(double a[9]) {
+    const double c00 = fma(a[4], a[8], -a[7] * a[5]);
+    const double c01 = fma(a[7], a[2], -a[1] * a[8]);
+    const double c02 = fma(a[1], a[5], -a[4] * a[2]);
+    const double det = fma(a[0], c00, fma(a[3], c01, a[6] * c02));
+    if (det == 0.0) return false;
+    const double r = 1.0 / det;
+    const double c10 = fma(a[6], a[5], -a[3] * a[8]);
+    const double c11 = fma(a[0], a[8], -a[6] * a[2]);
+    const double c12 = fma(a[3], a[2], -a[0] * a[5]);
+    const double c20 = fma(a[3], a[7], -a[6] * a[4]);
+    const double c21 = fma(a[6], a[1], -a[0] * a[7]);
+    const double c22 = fma(a[0], a[4], -a[3] * a[1]);
+    // inverse(i,j) = cofactor(j,i) / det, column-major
+    a[0] = c00 * r; a[1] = c01 * r; a[2] = c02 * r;
+    a[3] = c10 * r; a[4] = c11 * r; a[5] = c12 * r;
+    a[6] = c20 * r; a[7] = c21 * r; a[8] = c22 * r;
+    return true;
+}
+
+}  // namespace mfem

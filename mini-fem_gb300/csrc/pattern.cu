@@ -329,6 +329,7 @@ void build_pattern(Context &c, int order) {
     c.hasPattern = true;
     c.hasElemPos = false;
     c.gather.built = false;
+    c.tiles.built = false;
 }
 
 __global__ void k_diag_from_pattern(const int *__restrict__ rowPtr, const int *__restrict__ col,
@@ -378,6 +379,7 @@ void adopt_pattern(Context &c, const int *hRow, const int *hCol, int nnz) {
     c.hasPattern = true;
     c.hasElemPos = false;
     c.gather.built = false;
+    c.tiles.built = false;
 }
 
 void build_elem_pos(Context &c) {

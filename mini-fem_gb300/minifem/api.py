@@ -153,6 +153,9 @@ class Assembler:
     def set_sliver_threshold(self, q: float):
         self._check(N.lib.mfem_set_sliver_threshold(self._h, float(q)))
 
+    def set_option(self, name: str, value: float):
+        self._check(N.lib.mfem_set_option(self._h, name.encode(), float(value)))
+
     def flagged(self) -> int:
         n = C.c_int()
         self._check(N.lib.mfem_get_flagged(self._h, C.byref(n)))

@@ -170,12 +170,17 @@ def test_colouring_is_valid(gpu):
         assert np.all(np.diff(perm[members]) == 1)
 
 
+@pytest.mark.parametrize("kernel,tile", [(0, None), (1, None), (1, (8, 128))])
 @pytest.mark.parametrize("op,n,jit,sliver", [("lap", 14, 0.2, 0.0), ("ela", 14, 0.2, 0.0),
                                               ("ela", 12, 0.45, 0.05)])
-def test_fp32_within_tolerance(gpu, op, n, jit, sliver):
+def test_fp32_within_tolerance(gpu, op, n, jit, sliver, kernel, tile):
     m = cube_mesh(n, seed=11, op=op, jitter=jit, sliver_fraction=sliver,
                   jump=1e6 if sliver else 1.0, nu_max=0.45 if sliver else 0.35)
     a = gpu(0)
+    a.set_option("fp32_kernel", kernel)
+    if tile:
+        a.set_option("tile_rows", tile[0])
+        a.set_option("tile_elems", tile[1])
     a.set_mesh(m.coord, m.elemToNode)
     row, col = a.create_nodeToNode("reference")
     a.set_coefficients(op, m.coef)
@@ -189,6 +194,14 @@ def test_fp32_within_tolerance(gpu, op, n, jit, sliver):
     assert err.max() < TOL_FP32, err.max()
     if sliver:
         assert a.flagged() > 0
+    # the preconditioner: FP64 inverse of the compensated diagonal blocks
+    p = a.prec()
+    assert np.all(np.isfinite(p))
+    rel = np.abs(p - ref["prec"]) / (np.abs(ref["prec"]).reshape(-1, d).max(axis=1).repeat(d) + 1e-300)
+    assert rel.max() < 1e-4
+    # deterministic: a second assembly gives the same bits
+    a.assembly(op, "fp32", "gather", prec=True)
+    assert a.values_f32().tobytes() == v32.astype(np.float32).tobytes()
 
 
 def test_reference_shaped_calls_bit_exact(gpu):
