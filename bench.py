@@ -35,7 +35,7 @@ sys.path.insert(0, os.path.join(ROOT, "mini-fem_gb300"))
 
 import numpy as np  # noqa: E402
 
-N_SIDE = 100
+N_SIDE = 100      # nodes per side of the benchmark cube (--n changes it for small cases)
 SEED = 2024
 WORKLOAD = "ela_cube100_5.8M_tets"
 METRIC = "ela assembly Melem/s @5.8M tets: FP32-batched vs FP64-plain; % HBM roofline"
@@ -140,6 +140,11 @@ def kernel_bytes(name, E, N, nnz, n_edge_units, fp32):
 def make_mesh(rank):
     from minifem.meshgen import cube_mesh
     return cube_mesh(N_SIDE, seed=SEED + rank, op="ela")
+
+
+def workload_name():
+    from minifem.meshgen import cube_sizes
+    return WORKLOAD if N_SIDE == 100 else f"ela_cube{N_SIDE}_{cube_sizes(N_SIDE)[0]}_tets"
 
 
 def run_ours(args, rank, world, local_rank):
@@ -259,7 +264,7 @@ def run_ours(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: jittered (+-0.2h), node-permuted 100^3 Kuhn cube, E log-uniform "
                 "[1e9,2e11], nu U[0.2,0.35], seeded",
-        "config": {"workload": WORKLOAD, "nbElem": E, "nbNodes": N, "nbEdges": nnz,
+        "config": {"workload": workload_name(), "nbElem": E, "nbNodes": N, "nbEdges": nnz,
                    "operator": "ela", "precision": "fp32 (Kahan sums, fp64 slivers + block inverse)",
                    "strategy": "gather", "l2": "flushed (512 MB write) before every timed step",
                    "parallelism": f"replicas x{world}"},
@@ -328,7 +333,7 @@ def run_reference(args, rank, world):
     return {"metric": METRIC, "value": v, "unit": "Melem/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "nbElem": E, "nbNodes": N, "nbEdges": nnz},
+            "config": {"workload": workload_name(), "nbElem": E, "nbNodes": N, "nbEdges": nnz},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "Melem/s", "cores": 1, "kind": "port",
                              "sample": "full mesh per step; the reference's REF path is serial "
@@ -345,7 +350,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--n", type=int, default=N_SIDE,
+                    help="nodes per cube side (100 = the benchmark mesh; smaller for profiling)")
     args = ap.parse_args()
+    globals()["N_SIDE"] = args.n
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
