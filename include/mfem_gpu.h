@@ -95,6 +95,13 @@ int mfem_set_pattern(mfem_context *ctx, const int *row, const int *col, int nbEd
 int mfem_coloring_creation(mfem_context *ctx, unsigned long long seed, int *colorPerm,
                            int *colorIndex, int capacity, int *nbColors);
 
+/* ---- node renumbering (no counterpart in the reference; it orders for locality
+ * with DC-lib's D&C permutations, src/main.cc:155-206) ------------------------ */
+/* Reverse Cuthill-McKee order of the current pattern's graph:
+ * newOfOld[nbNodes], a permutation.  The caller renumbers coord and elemToNode
+ * with it and sets the renumbered mesh. */
+int mfem_rcm_permutation(mfem_context *ctx, int *newOfOld);
+
 /* ---- assembly: replaces assembly (src/assembly.cc:615-720) ------------------ */
 /* coef == NULL: the reference operator (constants 1 / 2.25, 1.25).  Otherwise
  * lap: kappa[nbElem]; ela: (E, nu)[nbElem*2], Young's modulus and Poisson ratio

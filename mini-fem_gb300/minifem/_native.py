@@ -36,6 +36,7 @@ _SIGS = {
     "mfem_create_elemToEdge": ([_vp, _vp], C.c_int),
     "mfem_set_pattern": ([_vp, _vp, _vp, C.c_int], C.c_int),
     "mfem_coloring_creation": ([_vp, C.c_ulonglong, _vp, _vp, C.c_int, _ip], C.c_int),
+    "mfem_rcm_permutation": ([_vp, _vp], C.c_int),
     "mfem_set_coefficients": ([_vp, C.c_int, _vp], C.c_int),
     "mfem_assemble": ([_vp, C.c_int, C.c_int, C.c_int], C.c_int),
     "mfem_assemble_prec": ([_vp, C.c_int, C.c_int, C.c_int], C.c_int),

@@ -125,6 +125,12 @@ class Assembler:
         self._check(N.lib.mfem_set_pattern(self._h, _ptr(row), _ptr(col), col.size))
         self.nbEdges = col.size
 
+    def rcm_permutation(self):
+        """newOfOld[N]: reverse Cuthill-McKee renumbering of the current pattern."""
+        out = np.empty(self.nbNodes, np.int32)
+        self._check(N.lib.mfem_rcm_permutation(self._h, _ptr(out)))
+        return out
+
     def create_elemToEdge(self):
         out = np.empty(self.nbElem * 16, np.int32)
         self._check(N.lib.mfem_create_elemToEdge(self._h, _ptr(out)))

@@ -210,6 +210,24 @@ def _make_slivers(coord, e2n, g, n, seed, fraction, max_aspect):
     return made
 
 
+def renumber_nodes(mesh: Mesh, newOfOld: np.ndarray) -> Mesh:
+    """The same mesh with node i renamed newOfOld[i] (elements keep their order)."""
+    newOfOld = np.asarray(newOfOld, dtype=np.int64)
+    coord = np.empty_like(mesh.coord)
+    coord[newOfOld] = mesh.coord
+    code = np.empty_like(mesh.boundNodesCode)
+    code[newOfOld] = mesh.boundNodesCode
+    e2n = (newOfOld[mesh.elemToNode - 1] + 1).astype(np.int32)
+    return Mesh(coord=coord, elemToNode=e2n, boundNodesCode=code, nbEdges=mesh.nbEdges,
+                coef=mesh.coef, op=mesh.op, meta=dict(mesh.meta, renumbered=True))
+
+
+def bandwidth(elemToNode: np.ndarray) -> int:
+    """max |i - j| over node pairs sharing an element."""
+    e = elemToNode.astype(np.int64)
+    return int((e.max(axis=1) - e.min(axis=1)).max())
+
+
 def write_reference_input(mesh: Mesh, path: str) -> None:
     """Write `mesh` in the binary layout that src/IO.cc:61-96 reads (one rank,
     no interfaces)."""

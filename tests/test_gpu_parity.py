@@ -265,3 +265,34 @@ def test_isolated_node_and_singular_block(gpu):
         ref = O.full(M, op=op, coef=None)
         assert vals.tobytes() == ref["values"].tobytes()
         assert prec.tobytes() == ref["prec"].tobytes()
+
+
+def test_rcm_renumbering_is_a_permutation_and_exact(gpu):
+    """RCM shrinks the bandwidth of the randomly numbered cube, and assembling the
+    renumbered mesh gives the permuted matrix bit for bit (same elements, same
+    order, same sums)."""
+    from minifem.meshgen import bandwidth, renumber_nodes
+    m = cube_mesh(10, seed=6, op="ela")
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    perm = a.rcm_permutation()
+    assert sorted(perm) == list(range(m.nbNodes))
+    r = renumber_nodes(m, perm)
+    assert bandwidth(r.elemToNode) < bandwidth(m.elemToNode) / 4
+    a.set_coefficients("ela", m.coef)
+    a.assembly("ela")
+    v = a.values().reshape(-1, 9)
+    b = gpu(0)
+    b.set_mesh(r.coord, r.elemToNode)
+    row2, col2 = b.create_nodeToNode("sorted")
+    b.set_coefficients("ela", m.coef)
+    b.assembly("ela")
+    v2 = b.values().reshape(-1, 9)
+    rr = np.repeat(np.arange(m.nbNodes), np.diff(row))
+    key_old = perm[rr].astype(np.int64) * m.nbNodes + perm[col - 1]
+    rr2 = np.repeat(np.arange(m.nbNodes), np.diff(row2))
+    key_new = rr2.astype(np.int64) * m.nbNodes + (col2 - 1)
+    o1, o2 = np.argsort(key_old), np.argsort(key_new)
+    assert np.array_equal(key_old[o1], key_new[o2])
+    assert v[o1].tobytes() == v2[o2].tobytes()
