@@ -137,6 +137,15 @@ def kernel_bytes(name, E, N, nnz, n_edge_units, fp32):
     return None
 
 
+# DRAM bytes per element of one launch, from `ncu --set full` captures of the 60^3
+# cube (profiles/tile32_ela_cube60.md, profiles/edge_units64_ela_cube60.md:
+# dram__bytes_read.sum + dram__bytes_write.sum divided by its 1,232,274 tets);
+# traffic grows in proportion to the mesh, so the full launch's traffic is this
+# times E.
+TRAFFIC_PER_ELEM = {"tile32+prec": (141.716992e6 + 97.9392e6) / 1232274,
+                    "edge_units64": (853.247744e6 + 244.699648e6) / 1232274}
+
+
 def make_mesh(rank):
     from minifem.meshgen import cube_mesh
     return cube_mesh(N_SIDE, seed=SEED + rank, op="ela")
@@ -248,8 +257,10 @@ def run_ours(args, rank, world, local_rank):
         kb = kernel_bytes(dom, E, N, nnz, n_edge, fp32)
         ach = kb / (ks[dom] * 1e-3) / 1e9
         sb = step_bytes(E, N, nnz, fp32)
+        tr = TRAFFIC_PER_ELEM.get(dom)
         return ({"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm,
-                 "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
+                 "unit": "GB/s", "frac": round(ach / hbm, 4),
+                 "traffic": round(tr * E) if tr else None,
                  "algorithmic_bytes": kb, "launch_ms": round(ks[dom], 4),
                  "peak_kind": peak_kind},
                 {"algorithmic_bytes": sb, "GB/s": round(sb / (step_ms * 1e-3) / 1e9, 1),

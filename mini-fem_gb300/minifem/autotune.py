@@ -1,0 +1,95 @@
+"""Autotuner: picks the assembly variant of a mesh by timing the candidates.
+
+Candidates (all produce results within the stated tolerances; the FP64 gather is
+the only bit-exact one, so a caller that needs bit-exactness keeps it):
+
+* FP32: kernel 0 (per-element gradient records + one thread per entry) or kernel 1
+  (spatial row tiles, gradients in shared memory) with tile sizes
+  (rows, elements) from TILE_CANDIDATES;
+* FP64: strategy gather / atomic / scatter (colour-ordered);
+* node numbering: identity or reverse Cuthill-McKee (the caller applies it, since
+  it renumbers the output).
+
+Each candidate runs `repeats` times after one warm-up; the median of the per-step
+device times (CUDA events recorded by the library around its launches) decides.
+Choices are cached in a JSON file keyed by the mesh sizes, operator, precision
+and device name, so a re-run on the same mesh reuses them without timing.
+"""
+from __future__ import annotations
+
+import json
+import os
+import statistics
+
+TILE_CANDIDATES = [(32, 320), (64, 640), (96, 960), (128, 1280)]
+
+
+def _device_name(device: int) -> str:
+    try:
+        import torch
+        return torch.cuda.get_device_name(device)
+    except Exception:
+        return "cuda"
+
+
+def _time(asm, op, precision, strategy, repeats):
+    asm.assembly(op, precision, strategy, prec=True)   # warm-up (and plan build)
+    asm.synchronize()
+    times = []
+    for _ in range(repeats):
+        asm.profile(True)
+        asm.assembly(op, precision, strategy, prec=True)
+        rec = asm.profile_read()
+        asm.profile(False)
+        times.append(sum(t for _, t in rec))
+    return statistics.median(times)
+
+
+def tune(asm, op: str, precision: str, repeats: int = 3, cache: str | None = None,
+         device: int = 0, strategies=None) -> dict:
+    """Time the candidates on `asm` (mesh, pattern, coefficients already set),
+    apply the fastest and return {"choice": ..., "ms": ..., "timings": [...]}."""
+    key = f"{asm.nbElem}:{asm.nbNodes}:{asm.nbEdges}:{op}:{precision}:{_device_name(device)}"
+    db = {}
+    if cache and os.path.exists(cache):
+        with open(cache) as f:
+            db = json.load(f)
+        if key in db:
+            _apply(asm, db[key]["choice"])
+            return db[key]
+    timings = []
+    if precision == "fp32":
+        asm.set_option("fp32_kernel", 0)
+        timings.append(({"fp32_kernel": 0, "strategy": "gather"},
+                        _time(asm, op, "fp32", "gather", repeats)))
+        for rows, elems in TILE_CANDIDATES:
+            asm.set_option("fp32_kernel", 1)
+            asm.set_option("tile_rows", rows)
+            asm.set_option("tile_elems", elems)
+            try:
+                t = _time(asm, op, "fp32", "gather", repeats)
+            except Exception:
+                continue   # a tile that cannot hold one row's elements
+            timings.append(({"fp32_kernel": 1, "tile_rows": rows, "tile_elems": elems,
+                             "strategy": "gather"}, t))
+    else:
+        for s in (strategies or ("gather", "atomic", "scatter")):
+            if s == "scatter":
+                asm.coloring_creation(seed=0)
+            timings.append(({"strategy": s}, _time(asm, op, "fp64", s, repeats)))
+    choice, ms = min(timings, key=lambda x: x[1])
+    _apply(asm, choice)
+    out = {"choice": choice, "ms": ms, "timings": [[c, t] for c, t in timings]}
+    if cache:
+        db[key] = out
+        tmp = cache + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(db, f, indent=1)
+        os.replace(tmp, cache)
+    return out
+
+
+def _apply(asm, choice: dict):
+    for k in ("fp32_kernel", "tile_rows", "tile_elems"):
+        if k in choice:
+            asm.set_option(k, choice[k])
