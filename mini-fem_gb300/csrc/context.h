@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "tiles.cuh"
 
 namespace mfem {
 
@@ -30,10 +31,11 @@ struct GatherPlan {
 // most maxRows rows touching at most maxElem elements.
 struct TilePlan {
     bool built = false;
-    int maxRows = 64, maxElem = 640;
+    int maxRows = 48, maxElem = 512;
     int nTiles = 0;
     long long nTileElems = 0;   // sum over tiles of their element counts
-    DevBuf desc, rows, elems, offPos, offMeta, diagMeta, contrib;
+    SmemLayout layout{};
+    DevBuf desc, elems, offEnt, diagEnt, contrib;
 };
 
 struct Coloring {
@@ -121,6 +123,8 @@ void build_gather_plan(Context &c);
 // tiles.cu
 void build_tile_plan(Context &c);
 void assemble_tiles32(Context &c, int op, bool fusePrec);
+TilePlanView plan_view(const TilePlan &tp);
+void split_coords(const Context &c, float4 *hi, float4 *lo, cudaStream_t s);
 
 // coloring.cu
 void build_coloring(Context &c, unsigned long long seed);

@@ -1,20 +1,23 @@
 // FP32 assembly by spatial tiles of rows (owner computes, one CTA per tile).
 //
 // The rows (nodes) are put in Morton order of their coordinates and cut into
-// tiles of at most kTileRows rows whose incident elements number at most
-// tileMaxElem.  One CTA per tile:
-//   1. computes the FP32 gradients and weights of every element incident to its
-//      rows (ascending element id) into shared memory -- each element once per
-//      tile that needs it, no gradient records in HBM;
-//   2. sums every off-diagonal entry of its rows from those gradients with Kahan
-//      compensation, one thread per entry, and writes it to the CSR values;
-//   3. sums the diagonal entries, writes them, and -- on the FP64 pipe, which
-//      runs beside the other warps' FP32 and memory work -- masks and inverts the
-//      3x3 (or 1x1) diagonal blocks into the preconditioner.
-// The plan (tile rows, tile elements, per-entry contribution lists as 16-bit
-// tile-local references) is built once per mesh on the host from the device
-// pattern; every list is in ascending element order, so results are
-// deterministic.
+// tiles of at most maxRows rows whose incident elements number at most maxElem.
+// One CTA per tile:
+//   0. one thread starts TMA bulk copies (cp.async.bulk, completion on an
+//      mbarrier) of the tile's contiguous plan segments -- contribution lists,
+//      off-diagonal entry table, diagonal table -- into shared memory;
+//   1. meanwhile every thread computes FP32 gradients and weights of the
+//      elements incident to the tile's rows (ascending element id) into shared
+//      memory: each element once per tile that needs it, no records in HBM;
+//   2. one thread per off-diagonal entry sums its contributions with Kahan
+//      compensation and writes the 3x3 block (or scalar) to the CSR values;
+//   3. four lanes per diagonal entry sum a quarter of its contributions each,
+//      combine them with error-free additions, write the block, and -- on the
+//      FP64 pipe, beside the other warps' FP32 and memory work -- mask and invert
+//      it into the preconditioner.
+// The plan is built once per mesh on the host from the device pattern.  Every
+// contribution list is in ascending element order and every combination order
+// is fixed, so results are deterministic.
 #include <algorithm>
 #include <cstdint>
 #include <numeric>
@@ -22,77 +25,131 @@
 
 #include "context.h"
 #include "elem32.cuh"
+#include "tiles.cuh"
 
 namespace mfem {
 
 namespace {
 
-constexpr int kTileThreads = 256;
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
 
-struct TileDesc {
-    int rowBegin, nRows;      // into tileRows
-    int elemBegin, nElem;     // into tileElems
-    int offBegin, nOff;       // into offPos / offMeta
-    int contribBegin, pad;    // into contrib16
-};
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
 
-uint32_t spread3(uint32_t v) {   // 10 bits -> every third bit
-    v &= 0x3ff;
-    v = (v | (v << 16)) & 0x030000FF;
-    v = (v | (v << 8)) & 0x0300F00F;
-    v = (v | (v << 4)) & 0x030C30C3;
-    v = (v | (v << 2)) & 0x09249249;
-    return v;
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 1D TMA bulk copy global -> shared; 16-byte aligned addresses, size % 16 == 0.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// error-free sum of two Kahan partials (value = s - c)
+__device__ __forceinline__ void kahan_merge(Kahan &a, float s2, float c2) {
+    const float s = a.s + s2;
+    const float bb = s - a.s;
+    const float err = (a.s - (s - bb)) + (s2 - bb);
+    a.c = (a.c + c2) - err;
+    a.s = s;
+}
+
+__device__ __forceinline__ void quad_combine(Kahan &k) {
+#pragma unroll
+    for (int off = 1; off <= 2; off <<= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, k.s, off);
+        const float c2 = __shfl_xor_sync(0xffffffffu, k.c, off);
+        kahan_merge(k, s2, c2);
+    }
 }
 
 template <int OP, bool PREC>
-__global__ void __launch_bounds__(kTileThreads)
-k_tile32(const TileDesc *__restrict__ tiles, const int *__restrict__ tileRows,
-         const int *__restrict__ tileElems, const int *__restrict__ offPos,
-         const unsigned *__restrict__ offMeta, const unsigned *__restrict__ diagMeta,
-         const unsigned short *__restrict__ contrib, const float4 *__restrict__ hi,
-         const float4 *__restrict__ lo, const double *__restrict__ coord,
-         const int4 *__restrict__ e2n, const double *__restrict__ coef,
-         const int *__restrict__ diagPos, const unsigned char *__restrict__ mask, float qthr2,
-         float *__restrict__ values, double *__restrict__ prec, int *counters) {
-    extern __shared__ float4 sm[];
-    const TileDesc T = tiles[blockIdx.x];
-    float4 *G = sm;                    // 4 per element: g_j.xyz
-    float4 *W = sm + 4 * T.nElem;      // 1 per element: (A, B, mu) or (kappa)
+__device__ __forceinline__ void tile_body(const TileDesc &T, const TileMesh &M, const TilePlanView &P,
+                                          const SmemLayout &L, float qthr2, unsigned char *sm,
+                                          int *counters) {
+    float4 *G = reinterpret_cast<float4 *>(sm);                       // 4 per element
+    float4 *W = reinterpret_cast<float4 *>(sm + L.w);                 // 1 per element
+    unsigned short *sC = reinterpret_cast<unsigned short *>(sm + L.contrib);
+    int2 *sOff = reinterpret_cast<int2 *>(sm + L.off);
+    int2 *sDiag = reinterpret_cast<int2 *>(sm + L.diag);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);
     const int tid = threadIdx.x;
+
+    // 0. stage the plan segments with the TMA engine
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        // make the initialised barrier visible to the TMA (async) proxy
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const unsigned bc = (unsigned)T.nContribPad * 2u, bo = (unsigned)T.nOffPad * 8u,
+                       bd = (unsigned)T.nRowsPad * 8u;
+        mbar_expect_tx(bar, bc + bo + bd);
+        if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar);
+        if (bo) bulk_g2s(sOff, P.offEnt + T.offBegin, bo, bar);
+        if (bd) bulk_g2s(sDiag, P.diagEnt + T.diagBegin, bd, bar);
+    }
 
     // 1. gradients of the tile's elements
     int flagged = 0;
     for (int i = tid; i < T.nElem; i += kTileThreads) {
-        const int e = tileElems[T.elemBegin + i];
+        const int e = P.elems[T.elemBegin + i];
         float g[12];
-        flagged += grad32(hi, lo, coord, e2n[e], qthr2, g);
+        flagged += grad32(M.hi, M.lo, M.coord, M.e2n[e], qthr2, g);
 #pragma unroll
         for (int j = 0; j < 4; j++) G[4 * i + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
-        W[i] = weights32<OP>(coef, e);
+        W[i] = weights32<OP>(M.coef, e);
     }
     if (flagged) atomicAdd(counters + 1, flagged);
     __syncthreads();
 
-    const unsigned short *cl = contrib + T.contribBegin;
+    // bounded wait for the staged segments (the CTA agrees on the outcome)
+    bool ok = false;
+    for (int it = 0; it < (1 << 22) && !ok; it++) ok = mbar_try_wait(bar, 0);
+    if (__syncthreads_or(!ok)) {
+        if (tid == 0) atomicOr(counters + 2, 1);
+        return;
+    }
+    if (tid == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+
     // 2. off-diagonal entries
     for (int t = tid; t < T.nOff; t += kTileThreads) {
-        const unsigned meta = offMeta[T.offBegin + t];
-        const int b = meta >> 8, n = meta & 0xff;
-        const int pos = offPos[T.offBegin + t];
+        const int2 ent = sOff[t];
+        const int b = (unsigned)ent.y >> 8, n = ent.y & 0xff;
         if (OP == MFEM_OP_LAP) {
             Kahan acc;
             for (int q = b; q < b + n; q++) {
-                const unsigned u = cl[q];
+                const unsigned u = sC[q];
                 const int l = u >> 4;
                 const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
                 acc.add(W[l].x * fmaf(gj.x, gk.x, fmaf(gj.y, gk.y, gj.z * gk.z)));
             }
-            values[pos] = acc.value();
+            M.values[ent.x] = acc.value();
         } else {
             Kahan acc[9];
             for (int q = b; q < b + n; q++) {
-                const unsigned u = cl[q];
+                const unsigned u = sC[q];
                 const int l = u >> 4;
                 const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
                 const float4 w = W[l];
@@ -107,32 +164,38 @@ k_tile32(const TileDesc *__restrict__ tiles, const int *__restrict__ tileRows,
                 acc[6].add(gj.z * gk.x * w.y);
                 acc[7].add(gj.z * gk.y * w.y);
             }
-            float *v = values + (size_t)pos * 9;
+            float *v = M.values + (size_t)ent.x * 9;
 #pragma unroll
             for (int m = 0; m < 9; m++) v[m] = acc[m].value();
         }
     }
 
-    // 3. diagonal entries + preconditioner
-    for (int t = tid; t < T.nRows; t += kTileThreads) {
-        const int r = tileRows[T.rowBegin + t];
-        const unsigned meta = diagMeta[T.rowBegin + t];
-        const int b = meta >> 8, n = meta & 0xff;
-        const int p = diagPos[r];
+    // 3. diagonal entries + preconditioner: four lanes per row
+    const int part = tid & 3;
+    for (int base = 0; base < T.nRows; base += kTileThreads / 4) {
+        const int rl = base + (tid >> 2);
+        const bool active = rl < T.nRows;
+        const int2 de = active ? sDiag[rl] : make_int2(0, 0);
+        const int r = de.x;
+        const int b = (unsigned)de.y >> 8, n = de.y & 0xff;
         if (OP == MFEM_OP_LAP) {
             Kahan acc;
-            for (int q = b; q < b + n; q++) {
-                const unsigned u = cl[q];
+            for (int q = b + part; q < b + n; q += 4) {
+                const unsigned u = sC[q];
                 const int l = u >> 4;
                 const float4 g = G[4 * l + ((u >> 2) & 3)];
                 acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
             }
-            if (p >= 0) values[p] = acc.value();
-            if (PREC) prec[r] = 1.0 / ((double)acc.s - (double)acc.c);
+            quad_combine(acc);
+            if (active && part == 0) {
+                const int p = M.diagPos[r];
+                if (p >= 0) M.values[p] = acc.value();
+                if (PREC) M.prec[r] = 1.0 / ((double)acc.s - (double)acc.c);
+            }
         } else {
             Kahan acc[6];
-            for (int q = b; q < b + n; q++) {
-                const unsigned u = cl[q];
+            for (int q = b + part; q < b + n; q += 4) {
+                const unsigned u = sC[q];
                 const int l = u >> 4;
                 const float4 g = G[4 * l + ((u >> 2) & 3)];
                 const float4 w = W[l];
@@ -144,27 +207,40 @@ k_tile32(const TileDesc *__restrict__ tiles, const int *__restrict__ tileRows,
                 acc[4].add(g.x * g.z * w.y);
                 acc[5].add(g.y * g.z * w.y);
             }
-            if (p >= 0) {
-                float *v = values + (size_t)p * 9;
-                const float d0 = acc[0].value(), d4 = acc[1].value(), d8 = acc[2].value();
-                const float o1 = acc[3].value(), o2 = acc[4].value(), o5 = acc[5].value();
-                v[0] = d0; v[1] = o1; v[2] = o2;
-                v[3] = o1; v[4] = d4; v[5] = o5;
-                v[6] = o2; v[7] = o5; v[8] = d8;
-            }
-            if (PREC) {
-                double s[6];
 #pragma unroll
-                for (int m = 0; m < 6; m++) s[m] = (double)acc[m].s - (double)acc[m].c;
-                double a[9] = {s[0], s[3], s[4], s[3], s[1], s[5], s[4], s[5], s[2]};
-                if (mask) dirichlet_mask3(a, mask[r]);
-                if (p >= 0 && !inv3_cofactor(a)) atomicAdd(counters, 1);
-                double *o = prec + (size_t)r * 9;   // 72-byte blocks: 8-byte aligned only
+            for (int m = 0; m < 6; m++) quad_combine(acc[m]);
+            if (active && part == 0) {
+                const int p = M.diagPos[r];
+                if (p >= 0) {
+                    float *v = M.values + (size_t)p * 9;
+                    const float d0 = acc[0].value(), d4 = acc[1].value(), d8 = acc[2].value();
+                    const float o1 = acc[3].value(), o2 = acc[4].value(), o5 = acc[5].value();
+                    v[0] = d0; v[1] = o1; v[2] = o2;
+                    v[3] = o1; v[4] = d4; v[5] = o5;
+                    v[6] = o2; v[7] = o5; v[8] = d8;
+                }
+                if (PREC) {
+                    double s[6];
 #pragma unroll
-                for (int m = 0; m < 9; m++) o[m] = a[m];
+                    for (int m = 0; m < 6; m++) s[m] = (double)acc[m].s - (double)acc[m].c;
+                    double a[9] = {s[0], s[3], s[4], s[3], s[1], s[5], s[4], s[5], s[2]};
+                    if (M.mask) dirichlet_mask3(a, M.mask[r]);
+                    if (p >= 0 && !inv3_cofactor(a)) atomicAdd(counters, 1);
+                    double *o = M.prec + (size_t)r * 9;   // 72-byte blocks: 8-byte aligned
+#pragma unroll
+                    for (int m = 0; m < 9; m++) o[m] = a[m];
+                }
             }
         }
     }
+}
+
+template <int OP, bool PREC>
+__global__ void __launch_bounds__(kTileThreads)
+k_tile32(TilePlanView P, TileMesh M, SmemLayout L, float qthr2, int *counters) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const TileDesc T = P.desc[blockIdx.x];
+    tile_body<OP, PREC>(T, M, P, L, qthr2, sm, counters);
 }
 
 __global__ void k_split_coords_t(const double *__restrict__ coord, int nbNodes,
@@ -178,7 +254,29 @@ __global__ void k_split_coords_t(const double *__restrict__ coord, int nbNodes,
                         __double2float_rn(z - (double)zh), 0.f);
 }
 
+uint32_t spread3(uint32_t v) {   // 10 bits -> every third bit
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x030000FF;
+    v = (v | (v << 8)) & 0x0300F00F;
+    v = (v | (v << 4)) & 0x030C30C3;
+    v = (v | (v << 2)) & 0x09249249;
+    return v;
+}
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
 }  // namespace
+
+SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad) {
+    SmemLayout L;
+    L.w = maxElem * 64;
+    L.contrib = L.w + maxElem * 16;
+    L.off = L.contrib + round_up(maxContribPad * 2, 16);
+    L.diag = L.off + maxOffPad * 8;
+    L.bar = L.diag + maxRowsPad * 8;
+    L.bytes = L.bar + 16;
+    return L;
+}
 
 // Host-side plan construction (once per mesh and pattern).
 void build_tile_plan(Context &c) {
@@ -198,7 +296,7 @@ void build_tile_plan(Context &c) {
     MFEM_CUDA(cudaMemcpyAsync(diagPos.data(), c.diagPos.ptr, diagPos.size() * 4, cudaMemcpyDeviceToHost, c.stream));
     MFEM_CUDA(cudaStreamSynchronize(c.stream));
 
-    // Morton order of the nodes
+    // Morton order of the nodes (10 bits per axis over the bounding box)
     double lo3[3] = {1e300, 1e300, 1e300}, hi3[3] = {-1e300, -1e300, -1e300};
     for (int i = 0; i < N; i++)
         for (int d = 0; d < 3; d++) {
@@ -210,7 +308,7 @@ void build_tile_plan(Context &c) {
         uint32_t q[3];
         for (int d = 0; d < 3; d++) {
             const double span = hi3[d] > lo3[d] ? hi3[d] - lo3[d] : 1.0;
-            double f = (coord[3 * (size_t)i + d] - lo3[d]) / span;
+            const double f = (coord[3 * (size_t)i + d] - lo3[d]) / span;
             q[d] = (uint32_t)std::min(1023.0, std::max(0.0, f * 1023.0));
         }
         const uint64_t m = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
@@ -219,34 +317,28 @@ void build_tile_plan(Context &c) {
     std::sort(key.begin(), key.end());
 
     std::vector<TileDesc> tiles;
-    std::vector<int> tileRows, tileElems, offPos;
-    std::vector<unsigned> offMeta, diagMeta;
+    std::vector<int> tileElems;
+    std::vector<int2> offEnt, diagEnt;
     std::vector<unsigned short> contrib;
-    tileRows.reserve(N);
-    offPos.reserve((size_t)nnz);
-    offMeta.reserve((size_t)nnz);
-    diagMeta.reserve(N);
-    contrib.reserve((size_t)E * 16 + 1024);
-    std::vector<int> mark(E, -1), local(E, 0);
-    std::vector<int> elems;
-    std::vector<int> cnt, fill;
+    offEnt.reserve((size_t)nnz + N);
+    diagEnt.reserve((size_t)N * 2);
+    contrib.reserve((size_t)E * 16 + (size_t)N);
+    std::vector<int> mark(E, -1), local(E, 0), elems, rows, cnt, fill, start;
+    int maxElem = 0, maxContrib = 0, maxOff = 0, maxRows = 0;
 
-    const int maxElem = tp.maxElem;
     int i = 0;
     while (i < N) {
         const int tIndex = (int)tiles.size();
         TileDesc T{};
-        T.rowBegin = (int)tileRows.size();
         elems.clear();
-        int nRows = 0;
-        // grow the tile
-        while (i < N && nRows < tp.maxRows) {
+        rows.clear();
+        while (i < N && (int)rows.size() < tp.maxRows) {
             const int r = (int)(key[i] & 0xffffffffu);
             int add = 0;
             for (int q = nptr[r]; q < nptr[r + 1]; q++)
                 if (mark[nelem[q] >> 2] != tIndex) add++;
-            if (nRows > 0 && (int)elems.size() + add > maxElem) break;
-            MFEM_REQUIRE((int)elems.size() + add <= maxElem, MFEM_ERR_CAPACITY,
+            if (!rows.empty() && (int)elems.size() + add > tp.maxElem) break;
+            MFEM_REQUIRE((int)elems.size() + add <= tp.maxElem, MFEM_ERR_CAPACITY,
                          "tile plan: one row touches more elements than a tile holds");
             for (int q = nptr[r]; q < nptr[r + 1]; q++) {
                 const int e = nelem[q] >> 2;
@@ -255,21 +347,19 @@ void build_tile_plan(Context &c) {
                     elems.push_back(e);
                 }
             }
-            tileRows.push_back(r);
-            nRows++;
+            rows.push_back(r);
             i++;
         }
         std::sort(elems.begin(), elems.end());
         for (int k = 0; k < (int)elems.size(); k++) local[elems[k]] = k;
-        T.nRows = nRows;
         T.elemBegin = (int)tileElems.size();
         T.nElem = (int)elems.size();
         tileElems.insert(tileElems.end(), elems.begin(), elems.end());
-        T.offBegin = (int)offPos.size();
+        T.offBegin = (int)offEnt.size();
+        T.diagBegin = (int)diagEnt.size();
         T.contribBegin = (int)contrib.size();
-        // contribution lists, row by row
-        for (int t = 0; t < nRows; t++) {
-            const int r = tileRows[T.rowBegin + t];
+        T.nRows = (int)rows.size();
+        for (int r : rows) {
             const int b = rowPtr[r], len = rowPtr[r + 1] - b;
             cnt.assign(len, 0);
             auto where = [&](int cc) {
@@ -285,7 +375,7 @@ void build_tile_plan(Context &c) {
                     cnt[m]++;
                 }
             }
-            std::vector<int> start(len + 1, 0);
+            start.assign(len + 1, 0);
             for (int m = 0; m < len; m++) start[m + 1] = start[m] + cnt[m];
             const int base = (int)contrib.size() - T.contribBegin;
             contrib.resize(contrib.size() + start[len]);
@@ -298,39 +388,69 @@ void build_tile_plan(Context &c) {
                         (unsigned short)((local[e] << 4) | (j << 2) | k);
                 }
             }
+            bool hasDiag = false;
             for (int m = 0; m < len; m++) {
-                MFEM_REQUIRE(cnt[m] <= 255 && base + start[m] < (1 << 24), MFEM_ERR_CAPACITY,
+                MFEM_REQUIRE(cnt[m] <= 255 && base + start[m] < (1 << 23), MFEM_ERR_CAPACITY,
                              "tile plan: too many contributions for one entry");
-                const unsigned meta = ((unsigned)(base + start[m]) << 8) | (unsigned)cnt[m];
+                const int meta = ((base + start[m]) << 8) | cnt[m];
                 if (col[b + m] == r) {
-                    diagMeta.push_back(meta);
+                    diagEnt.push_back(make_int2(r, meta));
+                    hasDiag = true;
                 } else {
-                    offPos.push_back(b + m);
-                    offMeta.push_back(meta);
+                    offEnt.push_back(make_int2(b + m, meta));
                 }
             }
-            if (diagPos[r] < 0) diagMeta.push_back(0u);
+            if (!hasDiag) diagEnt.push_back(make_int2(r, 0));
         }
-        T.nOff = (int)offPos.size() - T.offBegin;
+        T.nOff = (int)offEnt.size() - T.offBegin;
+        T.nContrib = (int)contrib.size() - T.contribBegin;
+        // pad every segment so that the next tile starts 16-byte aligned and
+        // the bulk copies move whole 16-byte units that lie inside the arrays
+        while (offEnt.size() % 2) offEnt.push_back(make_int2(0, 0));
+        while (diagEnt.size() % 2) diagEnt.push_back(make_int2(0, 0));
+        while (contrib.size() % 8) contrib.push_back(0);
+        T.nOffPad = (int)offEnt.size() - T.offBegin;
+        T.nRowsPad = (int)diagEnt.size() - T.diagBegin;
+        T.nContribPad = (int)contrib.size() - T.contribBegin;
+        maxElem = std::max(maxElem, T.nElem);
+        maxContrib = std::max(maxContrib, T.nContribPad);
+        maxOff = std::max(maxOff, T.nOffPad);
+        maxRows = std::max(maxRows, T.nRowsPad);
         tiles.push_back(T);
     }
-    MFEM_REQUIRE(tp.maxElem * 16 <= (1 << 16), MFEM_ERR_CAPACITY, "tile plan: local index overflow");
+    MFEM_REQUIRE(tp.maxElem <= 4096, MFEM_ERR_CAPACITY, "tile plan: local index overflow");
 
     tp.nTiles = (int)tiles.size();
+    tp.layout = smem_layout(std::max(maxElem, 1), maxContrib, maxOff, maxRows);
+    MFEM_REQUIRE(tp.layout.bytes <= 227 * 1024, MFEM_ERR_CAPACITY,
+                 "tile plan: a tile needs more than 227 KB of shared memory");
     auto up = [&](DevBuf &d, const void *src, size_t bytes) {
-        d.reserve(bytes);
-        MFEM_CUDA(cudaMemcpyAsync(d.ptr, src, bytes, cudaMemcpyHostToDevice, c.stream));
+        d.reserve(std::max<size_t>(bytes, 16));
+        if (bytes) MFEM_CUDA(cudaMemcpyAsync(d.ptr, src, bytes, cudaMemcpyHostToDevice, c.stream));
     };
     up(tp.desc, tiles.data(), tiles.size() * sizeof(TileDesc));
-    up(tp.rows, tileRows.data(), tileRows.size() * 4);
     up(tp.elems, tileElems.data(), tileElems.size() * 4);
-    up(tp.offPos, offPos.data(), std::max<size_t>(offPos.size(), 1) * 4);
-    up(tp.offMeta, offMeta.data(), std::max<size_t>(offMeta.size(), 1) * 4);
-    up(tp.diagMeta, diagMeta.data(), diagMeta.size() * 4);
-    up(tp.contrib, contrib.data(), std::max<size_t>(contrib.size(), 1) * 2);
+    up(tp.offEnt, offEnt.data(), offEnt.size() * sizeof(int2));
+    up(tp.diagEnt, diagEnt.data(), diagEnt.size() * sizeof(int2));
+    up(tp.contrib, contrib.data(), contrib.size() * 2);
     MFEM_CUDA(cudaStreamSynchronize(c.stream));
     tp.nTileElems = (long long)tileElems.size();
     tp.built = true;
+}
+
+TilePlanView plan_view(const TilePlan &tp) {
+    TilePlanView P;
+    P.desc = tp.desc.as<TileDesc>();
+    P.elems = tp.elems.as<int>();
+    P.offEnt = tp.offEnt.as<int2>();
+    P.diagEnt = tp.diagEnt.as<int2>();
+    P.contrib = tp.contrib.as<unsigned short>();
+    return P;
+}
+
+void split_coords(const Context &c, float4 *hi, float4 *lo, cudaStream_t s) {
+    k_split_coords_t<<<blocks_for(c.nbNodes, 256), 256, 0, s>>>(c.coord.as<double>(), c.nbNodes, hi, lo);
+    check_launch("k_split_coords_t");
 }
 
 void assemble_tiles32(Context &c, int op, bool fusePrec) {
@@ -343,23 +463,27 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     float4 *hi = (float4 *)c.scratch.reserve(sizeof(float4) * 2 * (size_t)N);
     float4 *lo = hi + N;
     c.timer.begin("split_coords", c.stream);
-    k_split_coords_t<<<blocks_for(N, 256), 256, 0, c.stream>>>(c.coord.as<double>(), N, hi, lo);
-    check_launch("k_split_coords_t");
+    split_coords(c, hi, lo, c.stream);
     c.timer.end(c.stream);
     int *st = status_ptr(c);
-    MFEM_CUDA(cudaMemsetAsync(st + 4, 0, sizeof(int) * 2, c.stream));
-    const size_t smem = (size_t)tp.maxElem * 5 * sizeof(float4);
-    const double *coef = c.coefOp == op ? c.coef.as<double>() : nullptr;
-    const unsigned char *mask = c.hasMask ? c.mask.as<unsigned char>() : nullptr;
+    MFEM_CUDA(cudaMemsetAsync(st + 4, 0, sizeof(int) * 3, c.stream));
+    TileMesh M;
+    M.hi = hi;
+    M.lo = lo;
+    M.coord = c.coord.as<double>();
+    M.e2n = c.e2n.as<int4>();
+    M.coef = c.coefOp == op ? c.coef.as<double>() : nullptr;
+    M.diagPos = c.diagPos.as<int>();
+    M.mask = c.hasMask ? c.mask.as<unsigned char>() : nullptr;
+    M.values = c.values.as<float>();
+    M.prec = prec;
+    const TilePlanView P = plan_view(tp);
+    const SmemLayout L = tp.layout;
     const float q = c.sliverThreshold;
     c.timer.begin(fusePrec ? "tile32+prec" : "tile32", c.stream);
     auto launch = [&](auto kern) {
-        MFEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<tp.nTiles, kTileThreads, smem, c.stream>>>(
-            tp.desc.as<TileDesc>(), tp.rows.as<int>(), tp.elems.as<int>(), tp.offPos.as<int>(),
-            tp.offMeta.as<unsigned>(), tp.diagMeta.as<unsigned>(), tp.contrib.as<unsigned short>(),
-            hi, lo, c.coord.as<double>(), c.e2n.as<int4>(), coef, c.diagPos.as<int>(), mask, q * q,
-            c.values.as<float>(), prec, st + 4);
+        MFEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+        kern<<<tp.nTiles, kTileThreads, L.bytes, c.stream>>>(P, M, L, q * q, st + 4);
     };
     if (op == MFEM_OP_LAP) {
         if (fusePrec) launch(k_tile32<MFEM_OP_LAP, true>);

@@ -1,0 +1,50 @@
+// Plan and argument structures of the FP32 tile kernel (tiles.cu, batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mfem {
+
+constexpr int kTileThreads = 256;
+
+// One tile: rows (diagonal table), elements, off-diagonal entries and the
+// contribution lists they reference.  Segment starts are 16-byte aligned and the
+// *Pad counts cover whole 16-byte units, so each segment is one bulk copy.
+struct TileDesc {
+    int diagBegin, nRows, nRowsPad;          // into diagEnt: (row, meta)
+    int elemBegin, nElem;                    // into elems
+    int offBegin, nOff, nOffPad;             // into offEnt: (CSR position, meta)
+    int contribBegin, nContrib, nContribPad; // into contrib (u16: local elem << 4 | j << 2 | k)
+    int mesh;                                // batch: index of the mesh the tile belongs to
+};
+
+// meta = (offset of the list in the tile's contributions) << 8 | list length
+
+struct TilePlanView {
+    const TileDesc *desc;
+    const int *elems;
+    const int2 *offEnt;
+    const int2 *diagEnt;
+    const unsigned short *contrib;
+};
+
+// Per-mesh device arrays the tile kernel reads and writes.
+struct TileMesh {
+    const float4 *hi, *lo;       // coordinates split into float hi + lo
+    const double *coord;         // FP64 coordinates (slivers)
+    const int4 *e2n;             // 0-based connectivity
+    const double *coef;          // per-element kappa or (E, nu); NULL: reference constants
+    const int *diagPos;
+    const unsigned char *mask;   // Dirichlet bits per node, or NULL
+    float *values;
+    double *prec;                // NULL: no preconditioner
+};
+
+// Byte offsets of the dynamic shared-memory regions.
+struct SmemLayout {
+    int w, contrib, off, diag, bar, bytes;
+};
+
+SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad);
+
+}  // namespace mfem

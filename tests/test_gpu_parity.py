@@ -296,3 +296,19 @@ def test_rcm_renumbering_is_a_permutation_and_exact(gpu):
     o1, o2 = np.argsort(key_old), np.argsort(key_new)
     assert np.array_equal(key_old[o1], key_new[o2])
     assert v[o1].tobytes() == v2[o2].tobytes()
+
+
+def test_autotuner_picks_a_valid_variant(gpu, tmp_path):
+    from minifem import autotune
+    m = cube_mesh(12, seed=3, op="ela")
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    a.create_nodeToNode("sorted")
+    a.set_coefficients("ela", m.coef)
+    cache = str(tmp_path / "tune.json")
+    r = autotune.tune(a, "ela", "fp32", repeats=2, cache=cache)
+    assert r["choice"]["strategy"] == "gather" and len(r["timings"]) >= 2
+    r2 = autotune.tune(a, "ela", "fp32", cache=cache)      # cached: no timing
+    assert r2["choice"] == r["choice"]
+    f = autotune.tune(a, "ela", "fp64", repeats=2)
+    assert f["choice"]["strategy"] in ("gather", "atomic", "scatter")
