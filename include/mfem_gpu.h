@@ -177,6 +177,35 @@ int mfem_get_sizes(mfem_context *ctx, int *nbElem, int *nbNodes, int *nbEdges,
 int mfem_assemble_noalloc(mfem_context *ctx, int operatorID, const double *coord,
                           const double *coef, double *values, void *stream);
 
+/* ---- batched assembly (no counterpart in the reference, which assembles one
+ * mesh per rank, src/FEM.cc:177-257) ------------------------------------------ */
+/* Many meshes (contexts with mesh, pattern and Dirichlet mask set; they must not
+ * change while in the batch), each with nbSets coefficient sets, assembled per
+ * iteration by one CUDA-graph replay: FP32 as ONE persistent launch over a
+ * cross-mesh work list of tiles, FP64 as the per-mesh, per-set gather launches.
+ * coefSets holds nbSets consecutive per-element arrays laid out as for
+ * mfem_set_coefficients (NULL only when nbSets == 1: reference constants). */
+typedef struct mfem_batch mfem_batch;
+int mfem_batch_create(mfem_batch **batch, int device);
+int mfem_batch_destroy(mfem_batch *batch);
+const char *mfem_batch_last_error(const mfem_batch *batch);
+int mfem_batch_get_stream(mfem_batch *batch, void **stream);
+int mfem_batch_add(mfem_batch *batch, mfem_context *ctx, int operatorID, int nbSets,
+                   const double *coefSets);
+/* New coefficients for item `item` (same layout and count as when added). */
+int mfem_batch_set_coefficients(mfem_batch *batch, int item, const double *coefSets);
+/* Enqueues one iteration (values of every set; the preconditioner too when
+ * withPrec != 0) on the batch stream.  mfem_batch_synchronize waits for it. */
+int mfem_batch_assemble(mfem_batch *batch, int precision, int withPrec);
+int mfem_batch_synchronize(mfem_batch *batch);
+/* values: nbEdges*opDim floats (MFEM_FP32) or doubles (MFEM_FP64). */
+int mfem_batch_get_values(mfem_batch *batch, int item, int set, int precision, void *values);
+int mfem_batch_get_prec(mfem_batch *batch, int item, int set, double *prec);
+/* Items, elements over all items, element-assemblies per iteration (elements x
+ * sets), work items and persistent grid size. */
+int mfem_batch_info(mfem_batch *batch, int *nbItems, long long *nbElemTotal,
+                    long long *nbAssemblies, int *nbWork, int *grid);
+
 /* ---- reference-shaped single calls (host buffers in and out) ---------------- */
 /* Same arguments and meaning as the reference operators; each call uploads what
  * it reads and downloads what it writes.  nodeToNodeRow / nodeToNodeColumn must

@@ -411,6 +411,41 @@ void gather_fp64_into(const Context &c, int op, const double *coord, const doubl
     check_launch("gather_fp64_into");
 }
 
+// FP64 gather of one coefficient set into caller-chosen buffers, with the fused
+// preconditioner when prec != NULL (batched assembly; same kernels and results
+// as assemble_fp64 with the gather strategy).
+void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec, double *values,
+                      double *prec, const unsigned char *mask, int *singular, cudaStream_t s) {
+    const GatherPlan &g = c.gather;
+    const int E = c.nbElem, N = c.nbNodes;
+    const int *dp = c.diagPos.as<int>(), *st = g.unitStart.as<int>();
+    const unsigned *ct = g.contrib.as<unsigned>();
+    const int2 *up = g.unitPos.as<int2>();
+    const int4 *e2n = c.e2n.as<int4>();
+    const double *coord = c.coord.as<double>();
+    auto run = [&](auto grad, auto diag, auto diagp, auto edge) {
+        grad<<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
+        if (prec)
+            diagp<<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, prec, mask, singular);
+        else
+            diag<<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+        if (g.nUnits > 0)
+            edge<<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
+    };
+    if (op == MFEM_OP_LAP) {
+        if (coef) run(k_grad64<MFEM_OP_LAP, true>, k_diag_units64<MFEM_OP_LAP, true, false>,
+                      k_diag_units64<MFEM_OP_LAP, true, true>, k_edge_units64<MFEM_OP_LAP, true>);
+        else run(k_grad64<MFEM_OP_LAP, false>, k_diag_units64<MFEM_OP_LAP, false, false>,
+                 k_diag_units64<MFEM_OP_LAP, false, true>, k_edge_units64<MFEM_OP_LAP, false>);
+    } else {
+        if (coef) run(k_grad64<MFEM_OP_ELA, true>, k_diag_units64<MFEM_OP_ELA, true, false>,
+                      k_diag_units64<MFEM_OP_ELA, true, true>, k_edge_units64<MFEM_OP_ELA, true>);
+        else run(k_grad64<MFEM_OP_ELA, false>, k_diag_units64<MFEM_OP_ELA, false, false>,
+                 k_diag_units64<MFEM_OP_ELA, false, true>, k_edge_units64<MFEM_OP_ELA, false>);
+    }
+    check_launch("gather_fp64_sets");
+}
+
 void prec_init_fp64(Context &c, int op) {
     const int dim = op == MFEM_OP_LAP ? 1 : 9;
     double *prec = (double *)c.prec.reserve(sizeof(double) * (size_t)c.nbNodes * dim);

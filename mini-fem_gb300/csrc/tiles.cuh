@@ -28,16 +28,25 @@ struct TilePlanView {
     const unsigned short *contrib;
 };
 
-// Per-mesh device arrays the tile kernel reads and writes.
+// Per-mesh geometry the tile kernel reads.
 struct TileMesh {
     const float4 *hi, *lo;       // coordinates split into float hi + lo
     const double *coord;         // FP64 coordinates (slivers)
     const int4 *e2n;             // 0-based connectivity
-    const double *coef;          // per-element kappa or (E, nu); NULL: reference constants
     const int *diagPos;
     const unsigned char *mask;   // Dirichlet bits per node, or NULL
+};
+
+// Coefficient sets of one mesh and where their results go: set s reads
+// coef + s*coefStride and writes values + s*valuesStride, prec + s*precStride.
+struct TileSets {
+    const double *coef;          // per-element kappa or (E, nu); NULL: reference constants
+    size_t coefStride;
     float *values;
+    size_t valuesStride;
     double *prec;                // NULL: no preconditioner
+    size_t precStride;
+    int nSets;
 };
 
 // Byte offsets of the dynamic shared-memory regions.

@@ -7,6 +7,6 @@ CPU fallback.
 """
 from ._native import (AUTO, ATOMIC, FP32, FP64, GATHER, OP_ELA, OP_LAP, ORDER_REFERENCE,  # noqa: F401
                       ORDER_SORTED, SCATTER, MfemError, lib)
-from .api import (Assembler, assembly, prec_init, prec_inversion, op_dim,  # noqa: F401
+from .api import (Assembler, Batch, assembly, prec_init, prec_inversion, op_dim,  # noqa: F401
                   op_id)
 from . import meshgen  # noqa: F401

@@ -56,6 +56,18 @@ _SIGS = {
     "mfem_profile_read": ([_vp, C.c_char_p, C.c_int, _fp, C.c_int, _ip], C.c_int),
     "mfem_get_sizes": ([_vp, _ip, _ip, _ip, _ip], C.c_int),
     "mfem_assemble_noalloc": ([_vp, C.c_int, _vp, _vp, _vp, _vp], C.c_int),
+    "mfem_batch_create": ([C.POINTER(_vp), C.c_int], C.c_int),
+    "mfem_batch_destroy": ([_vp], C.c_int),
+    "mfem_batch_last_error": ([_vp], C.c_char_p),
+    "mfem_batch_get_stream": ([_vp, C.POINTER(_vp)], C.c_int),
+    "mfem_batch_add": ([_vp, _vp, C.c_int, C.c_int, _vp], C.c_int),
+    "mfem_batch_set_coefficients": ([_vp, C.c_int, _vp], C.c_int),
+    "mfem_batch_assemble": ([_vp, C.c_int, C.c_int], C.c_int),
+    "mfem_batch_synchronize": ([_vp], C.c_int),
+    "mfem_batch_get_values": ([_vp, C.c_int, C.c_int, C.c_int, _vp], C.c_int),
+    "mfem_batch_get_prec": ([_vp, C.c_int, C.c_int, _vp], C.c_int),
+    "mfem_batch_info": ([_vp, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _ip, _ip],
+                        C.c_int),
     "mfem_assembly": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int],
                       C.c_int),
     "mfem_prec_init_host": ([_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int], C.c_int),

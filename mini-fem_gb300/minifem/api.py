@@ -217,6 +217,85 @@ class Assembler:
         return p.value, prec.value
 
 
+class Batch:
+    """Several meshes (Assemblers) x coefficient sets assembled per iteration by one
+    CUDA-graph replay (FP32: one persistent launch over all tiles)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        rc = N.lib.mfem_batch_create(C.byref(h), device)
+        if rc != N.MFEM_OK:
+            raise N.MfemError(rc, N.lib.mfem_status_string(rc).decode())
+        self._h = h
+        self.items = []
+        self._keep = []
+
+    def _check(self, rc):
+        if rc != N.MFEM_OK:
+            raise N.MfemError(rc, N.lib.mfem_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib.mfem_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(N.lib.mfem_batch_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def add(self, asm: Assembler, op, coef_sets=None):
+        """coef_sets: array [nSets, ...per-element coefficients...] or None."""
+        if coef_sets is None:
+            n, ptr = 1, None
+        else:
+            cs = _f64(coef_sets)
+            n = cs.shape[0]
+            self._keep.append(cs)
+            ptr = _ptr(cs)
+        self._check(N.lib.mfem_batch_add(self._h, asm._h, op_id(op), n, ptr))
+        self.items.append((asm, op_id(op), n))
+        return len(self.items) - 1
+
+    def set_coefficients(self, item: int, coef_sets):
+        cs = _f64(coef_sets)
+        self._keep.append(cs)
+        self._check(N.lib.mfem_batch_set_coefficients(self._h, item, _ptr(cs)))
+
+    def assemble(self, precision: str = "fp32", prec: bool = True):
+        self._check(N.lib.mfem_batch_assemble(self._h, _PRECISIONS[precision], 1 if prec else 0))
+
+    def synchronize(self):
+        self._check(N.lib.mfem_batch_synchronize(self._h))
+
+    def values(self, item: int, set_: int, precision: str = "fp32"):
+        asm, op, _ = self.items[item]
+        out = np.empty(asm.nbEdges * op_dim(op), np.float32 if precision == "fp32" else np.float64)
+        self._check(N.lib.mfem_batch_get_values(self._h, item, set_, _PRECISIONS[precision],
+                                                _ptr(out)))
+        return out
+
+    def prec(self, item: int, set_: int):
+        asm, op, _ = self.items[item]
+        out = np.empty(asm.nbNodes * op_dim(op), np.float64)
+        self._check(N.lib.mfem_batch_get_prec(self._h, item, set_, _ptr(out)))
+        return out
+
+    def info(self):
+        ni, e, asmb, w, g = C.c_int(), C.c_longlong(), C.c_longlong(), C.c_int(), C.c_int()
+        self._check(N.lib.mfem_batch_info(self._h, C.byref(ni), C.byref(e), C.byref(asmb),
+                                          C.byref(w), C.byref(g)))
+        return {"items": ni.value, "elements": e.value, "assemblies": asmb.value,
+                "work": w.value, "grid": g.value}
+
+
 # ---- reference-shaped calls on a shared default context ---------------------------
 
 _default: Assembler | None = None

@@ -312,3 +312,38 @@ def test_autotuner_picks_a_valid_variant(gpu, tmp_path):
     assert r2["choice"] == r["choice"]
     f = autotune.tune(a, "ela", "fp64", repeats=2)
     assert f["choice"]["strategy"] in ("gather", "atomic", "scatter")
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batch_equals_single_mesh_entry_points(gpu, precision):
+    """Meshes of uneven size, lap and ela, several coefficient sets each: every
+    (mesh, set) of one batched iteration equals the single-mesh entry point bit
+    for bit (same plans, same arithmetic)."""
+    import minifem
+    specs = [(5, "lap", 2), (9, "ela", 3), (7, "ela", 1), (11, "lap", 2)]
+    b = minifem.Batch(0)
+    asms, sets = [], []
+    for n, op, k in specs:
+        meshes = [cube_mesh(n, seed=100 * n + s, op=op) for s in range(k)]
+        m = meshes[0]
+        a = gpu(0)
+        a.set_mesh(m.coord, m.elemToNode)
+        a.create_nodeToNode("sorted")
+        a.set_check_bounds(O.checkbounds(m.boundNodesCode))
+        cs = np.stack([mm.coef for mm in meshes])
+        b.add(a, op, cs)
+        asms.append((a, op))
+        sets.append(cs)
+    info = b.info()
+    assert info["items"] == len(specs)
+    for it in range(2):                      # graph replays
+        b.assemble(precision, prec=True)
+        b.synchronize()
+    for i, ((a, op), cs) in enumerate(zip(asms, sets)):
+        for s in range(cs.shape[0]):
+            a.set_coefficients(op, cs[s])
+            a.assembly(op, precision, "gather", prec=True)
+            ref_v = a.values_f32() if precision == "fp32" else a.values()
+            got = b.values(i, s, precision)
+            assert got.tobytes() == ref_v.tobytes(), (i, s)
+            assert b.prec(i, s).tobytes() == a.prec().tobytes(), (i, s)
