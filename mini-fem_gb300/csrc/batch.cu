@@ -97,7 +97,7 @@ void prepare(mfem_batch &b) {
     MFEM_REQUIRE(!b.items.empty(), MFEM_ERR_STATE, "empty batch");
     // sizes and offsets
     b.totalVal = b.totalPrec = b.totalNodes = 0;
-    int maxW = 0, maxC = 0, maxO = 0, maxD = 0;
+    int maxW = 0, maxWW = 0, maxC = 0, maxO = 0, maxD = 0, maxR = 0;
     std::vector<TileDesc> all;
     std::vector<long long> cost;
     size_t maxRec = 0;
@@ -114,10 +114,12 @@ void prepare(mfem_batch &b) {
         b.totalNodes += (size_t)c.nbNodes;
         maxRec = std::max(maxRec, (size_t)c.nbElem * 16);
         const SmemLayout &L = c.tiles.layout;
-        maxW = std::max(maxW, L.contrib);
+        maxW = std::max(maxW, L.w);
+        maxWW = std::max(maxWW, L.contrib - L.w);
         maxC = std::max(maxC, L.off - L.contrib);
         maxO = std::max(maxO, L.diag - L.off);
-        maxD = std::max(maxD, L.bar - L.diag);
+        maxD = std::max(maxD, L.res - L.diag);
+        maxR = std::max(maxR, L.bar - L.res);
         std::vector<TileDesc> d(c.tiles.nTiles);
         MFEM_CUDA(cudaMemcpy(d.data(), c.tiles.desc.ptr, sizeof(TileDesc) * d.size(), cudaMemcpyDeviceToHost));
         for (auto &t : d) {
@@ -126,13 +128,14 @@ void prepare(mfem_batch &b) {
             cost.push_back((long long)t.nElem * 4 + (long long)t.nContrib * it->nSets);
         }
     }
-    // shared-memory layout holding any tile of any mesh (G + W regions scale together)
+    // shared-memory layout holding any tile of any mesh: region-wise maxima
     SmemLayout L;
-    L.w = maxW / 80 * 64;
-    L.contrib = maxW;
+    L.w = maxW;
+    L.contrib = L.w + maxWW;
     L.off = L.contrib + maxC;
     L.diag = L.off + maxO;
-    L.bar = L.diag + maxD;
+    L.res = L.diag + maxD;
+    L.bar = L.res + maxR;
     L.bytes = L.bar + 16;
     b.layout = L;
     MFEM_REQUIRE(L.bytes <= 227 * 1024, MFEM_ERR_CAPACITY, "batch: tiles need more than 227 KB");

@@ -55,17 +55,32 @@ __device__ __forceinline__ bool grad32(const float4 *__restrict__ hi, const floa
     return false;
 }
 
-// Weights (A, B, mu) of the elasticity blocks, or (kappa, -, -) for lap, in FP32
-// from the FP64 per-element coefficients (NULL: the reference constants).
+// double -> float, round to nearest even, with integer operations so that it
+// stays off GB300's narrow FP64 pipe; values outside the normal float range
+// (and zero) take the conversion instruction.
+__device__ __forceinline__ float f64_to_f32(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if (e <= 1023u - 127u || e >= 1023u + 127u) return __double2float_rn(x);
+    const unsigned m23 = ((hi & 0xfffffu) << 3) | (lo >> 29);   // top 23 mantissa bits
+    const unsigned rem = lo & 0x1fffffffu;                        // the 29 bits dropped
+    unsigned r = (hi & 0x80000000u) | ((e - 1023u + 127u) << 23) | m23;
+    if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;   // carries into the exponent
+    return __uint_as_float(r);
+}
+
+// Weights of the FP32 blocks: (B, mu) = (lambda + mu, mu) for ela, (kappa, 0)
+// for lap, in FP32 from the FP64 per-element coefficients (NULL: the reference
+// constants B = 1.25, mu = 1, kappa = 1).
 template <int OP>
-__device__ __forceinline__ float4 weights32(const double *__restrict__ coef, int e) {
-    if (OP == MFEM_OP_LAP) return make_float4(coef ? __double2float_rn(coef[e]) : 1.0f, 0.f, 0.f, 0.f);
-    if (!coef) return make_float4(2.25f, 1.25f, 1.0f, 0.f);
+__device__ __forceinline__ float2 weights32(const double *__restrict__ coef, int e) {
+    if (OP == MFEM_OP_LAP) return make_float2(coef ? f64_to_f32(coef[e]) : 1.0f, 0.f);
+    if (!coef) return make_float2(1.25f, 1.0f);
     const double2 c = reinterpret_cast<const double2 *>(coef)[e];
-    const float E = __double2float_rn(c.x), nu = __double2float_rn(c.y);
+    const float E = f64_to_f32(c.x), nu = f64_to_f32(c.y);
     const float lam = (E * nu) / ((1.0f + nu) * (1.0f - 2.0f * nu));
     const float mu = E / (2.0f * (1.0f + nu));
-    return make_float4(fmaf(2.0f, mu, lam), lam + mu, mu, 0.f);
+    return make_float2(lam + mu, mu);
 }
 
 struct Kahan {

@@ -65,6 +65,69 @@ __device__ __forceinline__ void quad_combine(Kahan &k) {
     }
 }
 
+// float -> double is exact; done with integer operations so that it does not
+// occupy GB300's narrow FP64 pipe (zero and subnormal inputs take the
+// conversion instruction).
+__device__ __forceinline__ double f32_to_f64(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const unsigned lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// One elasticity contribution (j, k) in the FP32 form
+//   c(a,b) = B gj_a gk_b + delta_ab mu (gj . gk)
+// which is the reference's ((p_aa A + p_bb mu) + p_cc mu), p_ab B with
+// A = B + mu, regrouped.  `first` assigns instead of accumulating (exact).
+__device__ __forceinline__ void ela_accumulate(Kahan *acc, float4 gj, float4 gk, float B, float mu,
+                                               bool first) {
+    const float bx = gk.x * B, by = gk.y * B, bz = gk.z * B;
+    const float md = mu * fmaf(gj.x, gk.x, fmaf(gj.y, gk.y, gj.z * gk.z));
+    const float c[9] = {fmaf(gj.x, bx, md), gj.x * by, gj.x * bz,
+                        gj.y * bx, fmaf(gj.y, by, md), gj.y * bz,
+                        gj.z * bx, gj.z * by, fmaf(gj.z, bz, md)};
+    if (first) {
+#pragma unroll
+        for (int m = 0; m < 9; m++) { acc[m].s = c[m]; acc[m].c = 0.f; }
+    } else {
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc[m].add(c[m]);
+    }
+}
+
+// Symmetric diagonal block (j, j): six distinct values d00, d11, d22, d01, d02, d12.
+__device__ __forceinline__ void ela_diag_accumulate(Kahan *acc, float4 g, float B, float mu) {
+    const float bx = g.x * B, by = g.y * B, bz = g.z * B;
+    const float md = mu * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z));
+    acc[0].add(fmaf(g.x, bx, md));
+    acc[1].add(fmaf(g.y, by, md));
+    acc[2].add(fmaf(g.z, bz, md));
+    acc[3].add(g.x * by);
+    acc[4].add(g.x * bz);
+    acc[5].add(g.y * bz);
+}
+
+// Inverse of a symmetric 3x3 block by its six distinct cofactors (FP64, FMAs);
+// d = (d00, d11, d22, d01, d02, d12).  Returns false for an exactly singular
+// block, which is then left as it is.
+__device__ __forceinline__ bool inv3_sym(double d[6]) {
+    const double a = d[0], e = d[1], i = d[2], b = d[3], c = d[4], f = d[5];
+    const double c00 = fma(e, i, -f * f);
+    const double c01 = fma(c, f, -b * i);
+    const double c02 = fma(b, f, -c * e);
+    const double det = fma(a, c00, fma(b, c01, c * c02));
+    if (det == 0.0) return false;
+    const double r = 1.0 / det;
+    const double c11 = fma(a, i, -c * c);
+    const double c12 = fma(b, c, -a * f);
+    const double c22 = fma(a, e, -b * b);
+    d[0] = c00 * r; d[1] = c11 * r; d[2] = c22 * r;
+    d[3] = c01 * r; d[4] = c02 * r; d[5] = c12 * r;
+    return true;
+}
+
 // One tile for nSets coefficient sets: the gradients are computed once, the
 // weights, entries and preconditioner blocks once per set.  Returns false when
 // the staged plan segments did not arrive within the bounded wait (error flag
@@ -74,10 +137,11 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                                           const TilePlanView &P, const SmemLayout &L, float qthr2,
                                           unsigned char *sm, int *counters) {
     float4 *G = reinterpret_cast<float4 *>(sm);                       // 4 per element
-    float4 *W = reinterpret_cast<float4 *>(sm + L.w);                 // 1 per element
+    float2 *W = reinterpret_cast<float2 *>(sm + L.w);                 // (B, mu) or (kappa, -)
     unsigned short *sC = reinterpret_cast<unsigned short *>(sm + L.contrib);
-    int2 *sOff = reinterpret_cast<int2 *>(sm + L.off);
+    int4 *sOff = reinterpret_cast<int4 *>(sm + L.off);
     int2 *sDiag = reinterpret_cast<int2 *>(sm + L.diag);
+    float *sRes = reinterpret_cast<float *>(sm + L.res);              // 12 floats per row
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);
     const int tid = threadIdx.x;
 
@@ -87,7 +151,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         // make the initialised barrier visible to the TMA (async) proxy
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const unsigned bc = (unsigned)T.nContribPad * 2u, bo = (unsigned)T.nOffPad * 8u,
+        const unsigned bc = (unsigned)T.nContribPad * 2u, bo = (unsigned)T.nOffPad * 16u,
                        bd = (unsigned)T.nRowsPad * 8u;
         mbar_expect_tx(bar, bc + bo + bd);
         if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar);
@@ -117,119 +181,142 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     }
     if (tid == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 
-  for (int set = 0; set < S.nSets; set++) {
-    float *values = S.values + (size_t)set * S.valuesStride;
-    double *precOut = S.prec ? S.prec + (size_t)set * S.precStride : nullptr;
-    if (set > 0) {
-        // weights of this set (every thread is done with the previous set's)
-        __syncthreads();
-        const double *coef = S.coef ? S.coef + (size_t)set * S.coefStride : nullptr;
-        for (int i = tid; i < T.nElem; i += kTileThreads)
-            W[i] = weights32<OP>(coef, P.elems[T.elemBegin + i]);
-        __syncthreads();
-    }
-
-    // 2. off-diagonal entries
-    for (int t = tid; t < T.nOff; t += kTileThreads) {
-        const int2 ent = sOff[t];
-        const int b = (unsigned)ent.y >> 8, n = ent.y & 0xff;
-        if (OP == MFEM_OP_LAP) {
-            Kahan acc;
-            for (int q = b; q < b + n; q++) {
-                const unsigned u = sC[q];
-                const int l = u >> 4;
-                const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
-                acc.add(W[l].x * fmaf(gj.x, gk.x, fmaf(gj.y, gk.y, gj.z * gk.z)));
-            }
-            values[ent.x] = acc.value();
-        } else {
-            Kahan acc[9];
-            for (int q = b; q < b + n; q++) {
-                const unsigned u = sC[q];
-                const int l = u >> 4;
-                const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
-                const float4 w = W[l];
-                const float p00 = gj.x * gk.x, p11 = gj.y * gk.y, p22 = gj.z * gk.z;
-                acc[0].add(fmaf(p00, w.x, (p11 + p22) * w.z));
-                acc[4].add(fmaf(p11, w.x, (p00 + p22) * w.z));
-                acc[8].add(fmaf(p22, w.x, (p00 + p11) * w.z));
-                acc[1].add(gj.x * gk.y * w.y);
-                acc[2].add(gj.x * gk.z * w.y);
-                acc[3].add(gj.y * gk.x * w.y);
-                acc[5].add(gj.y * gk.z * w.y);
-                acc[6].add(gj.z * gk.x * w.y);
-                acc[7].add(gj.z * gk.y * w.y);
-            }
-            float *v = values + (size_t)ent.x * 9;
-#pragma unroll
-            for (int m = 0; m < 9; m++) v[m] = acc[m].value();
+    for (int set = 0; set < S.nSets; set++) {
+        float *values = S.values + (size_t)set * S.valuesStride;
+        double *precOut = S.prec ? S.prec + (size_t)set * S.precStride : nullptr;
+        if (set > 0) {
+            // weights of this set (every thread is done with the previous set's)
+            __syncthreads();
+            const double *coef = S.coef ? S.coef + (size_t)set * S.coefStride : nullptr;
+            for (int i = tid; i < T.nElem; i += kTileThreads)
+                W[i] = weights32<OP>(coef, P.elems[T.elemBegin + i]);
+            __syncthreads();
         }
-    }
 
-    // 3. diagonal entries + preconditioner: four lanes per row
-    const int part = tid & 3;
-    for (int base = 0; base < T.nRows; base += kTileThreads / 4) {
-        const int rl = base + (tid >> 2);
-        const bool active = rl < T.nRows;
-        const int2 de = active ? sDiag[rl] : make_int2(0, 0);
-        const int r = de.x;
-        const int b = (unsigned)de.y >> 8, n = de.y & 0xff;
-        if (OP == MFEM_OP_LAP) {
-            Kahan acc;
-            for (int q = b + part; q < b + n; q += 4) {
-                const unsigned u = sC[q];
-                const int l = u >> 4;
-                const float4 g = G[4 * l + ((u >> 2) & 3)];
-                acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
-            }
-            quad_combine(acc);
-            if (active && part == 0) {
-                const int p = M.diagPos[r];
-                if (p >= 0) values[p] = acc.value();
-                if (PREC) precOut[r] = 1.0 / ((double)acc.s - (double)acc.c);
-            }
-        } else {
-            Kahan acc[6];
-            for (int q = b + part; q < b + n; q += 4) {
-                const unsigned u = sC[q];
-                const int l = u >> 4;
-                const float4 g = G[4 * l + ((u >> 2) & 3)];
-                const float4 w = W[l];
-                const float p00 = g.x * g.x, p11 = g.y * g.y, p22 = g.z * g.z;
-                acc[0].add(fmaf(p00, w.x, (p11 + p22) * w.z));
-                acc[1].add(fmaf(p11, w.x, (p00 + p22) * w.z));
-                acc[2].add(fmaf(p22, w.x, (p00 + p11) * w.z));
-                acc[3].add(g.x * g.y * w.y);
-                acc[4].add(g.x * g.z * w.y);
-                acc[5].add(g.y * g.z * w.y);
-            }
+        // 2. off-diagonal units: entry (r, c) and, when c is a row of this tile,
+        //    its transpose (c, r), which is the same sum transposed
+        for (int t = tid; t < T.nOff; t += kTileThreads) {
+            const int4 ent = sOff[t];
+            const int b = (unsigned)ent.z >> 8, n = ent.z & 0xff;
+            if (OP == MFEM_OP_LAP) {
+                Kahan acc;
+                for (int q = b; q < b + n; q++) {
+                    const unsigned u = sC[q];
+                    const int l = u >> 4;
+                    const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
+                    const float x = W[l].x * fmaf(gj.x, gk.x, fmaf(gj.y, gk.y, gj.z * gk.z));
+                    if (q == b) { acc.s = x; acc.c = 0.f; } else acc.add(x);
+                }
+                const float v = acc.value();
+                values[ent.x] = v;
+                if (ent.y >= 0) values[ent.y] = v;
+            } else {
+                Kahan acc[9];
+                for (int q = b; q < b + n; q++) {
+                    const unsigned u = sC[q];
+                    const int l = u >> 4;
+                    const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
+                    const float2 w = W[l];
+                    ela_accumulate(acc, gj, gk, w.x, w.y, q == b);
+                }
+                float v[9];
 #pragma unroll
-            for (int m = 0; m < 6; m++) quad_combine(acc[m]);
-            if (active && part == 0) {
-                const int p = M.diagPos[r];
+                for (int m = 0; m < 9; m++) v[m] = n ? acc[m].value() : 0.f;
+                float *o = values + (size_t)ent.x * 9;
+#pragma unroll
+                for (int m = 0; m < 9; m++) o[m] = v[m];
+                if (ent.y >= 0) {
+                    float *tr = values + (size_t)ent.y * 9;
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+#pragma unroll
+                        for (int bb = 0; bb < 3; bb++) tr[3 * bb + a] = v[3 * a + bb];
+                }
+            }
+        }
+
+        // 3a. diagonal entries: four lanes per row, combined without error
+        const int part = tid & 3;
+        for (int base = 0; base < T.nRows; base += kTileThreads / 4) {
+            const int rl = base + (tid >> 2);
+            const bool active = rl < T.nRows;
+            const int2 de = active ? sDiag[rl] : make_int2(0, 0);
+            const int b = (unsigned)de.y >> 8, n = de.y & 0xff;
+            if (OP == MFEM_OP_LAP) {
+                Kahan acc;
+                for (int q = b + part; q < b + n; q += 4) {
+                    const unsigned u = sC[q];
+                    const int l = u >> 4;
+                    const float4 g = G[4 * l + ((u >> 2) & 3)];
+                    acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
+                }
+                quad_combine(acc);
+                if (active && part == 0) {
+                    sRes[12 * rl] = acc.s;
+                    sRes[12 * rl + 1] = acc.c;
+                }
+            } else {
+                Kahan acc[6];
+                for (int q = b + part; q < b + n; q += 4) {
+                    const unsigned u = sC[q];
+                    const int l = u >> 4;
+                    const float2 w = W[l];
+                    ela_diag_accumulate(acc, G[4 * l + ((u >> 2) & 3)], w.x, w.y);
+                }
+#pragma unroll
+                for (int m = 0; m < 6; m++) quad_combine(acc[m]);
+                if (active && part == 0) {
+#pragma unroll
+                    for (int m = 0; m < 6; m++) {
+                        sRes[12 * rl + 2 * m] = acc[m].s;
+                        sRes[12 * rl + 2 * m + 1] = acc[m].c;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // 3b. one thread per row: write the diagonal block and the preconditioner
+        //     (full warps on the FP64 pipe)
+        for (int rl = tid; rl < T.nRows; rl += kTileThreads) {
+            const int r = sDiag[rl].x;
+            const int p = M.diagPos[r];
+            if (OP == MFEM_OP_LAP) {
+                const float s = sRes[12 * rl], c = sRes[12 * rl + 1];
+                if (p >= 0) values[p] = s - c;
+                if (PREC) precOut[r] = 1.0 / (f32_to_f64(s) - f32_to_f64(c));
+            } else {
+                float sv[6];
+                double d[6];
+#pragma unroll
+                for (int m = 0; m < 6; m++) {
+                    const float s = sRes[12 * rl + 2 * m], c = sRes[12 * rl + 2 * m + 1];
+                    sv[m] = s - c;
+                    if (PREC) d[m] = f32_to_f64(s) - f32_to_f64(c);
+                }
                 if (p >= 0) {
                     float *v = values + (size_t)p * 9;
-                    const float d0 = acc[0].value(), d4 = acc[1].value(), d8 = acc[2].value();
-                    const float o1 = acc[3].value(), o2 = acc[4].value(), o5 = acc[5].value();
-                    v[0] = d0; v[1] = o1; v[2] = o2;
-                    v[3] = o1; v[4] = d4; v[5] = o5;
-                    v[6] = o2; v[7] = o5; v[8] = d8;
+                    v[0] = sv[0]; v[1] = sv[3]; v[2] = sv[4];
+                    v[3] = sv[3]; v[4] = sv[1]; v[5] = sv[5];
+                    v[6] = sv[4]; v[7] = sv[5]; v[8] = sv[2];
                 }
                 if (PREC) {
-                    double s[6];
-#pragma unroll
-                    for (int m = 0; m < 6; m++) s[m] = (double)acc[m].s - (double)acc[m].c;
-                    double a[9] = {s[0], s[3], s[4], s[3], s[1], s[5], s[4], s[5], s[2]};
-                    if (M.mask) dirichlet_mask3(a, M.mask[r]);
-                    if (p >= 0 && !inv3_cofactor(a)) atomicAdd(counters, 1);
+                    if (M.mask) {
+                        // src/Fortran/elasclpr.f:19-27: constrained DOF k -> row and
+                        // column k of the block zero, diagonal 1
+                        const unsigned mk = M.mask[r];
+                        if (mk & 1u) { d[0] = 1.0; d[3] = 0.0; d[4] = 0.0; }
+                        if (mk & 2u) { d[1] = 1.0; d[3] = 0.0; d[5] = 0.0; }
+                        if (mk & 4u) { d[2] = 1.0; d[4] = 0.0; d[5] = 0.0; }
+                    }
+                    if (p >= 0 && !inv3_sym(d)) atomicAdd(counters, 1);
                     double *o = precOut + (size_t)r * 9;   // 72-byte blocks: 8-byte aligned
-#pragma unroll
-                    for (int m = 0; m < 9; m++) o[m] = a[m];
+                    o[0] = d[0]; o[1] = d[3]; o[2] = d[4];
+                    o[3] = d[3]; o[4] = d[1]; o[5] = d[5];
+                    o[6] = d[4]; o[7] = d[5]; o[8] = d[2];
                 }
             }
         }
     }
-  }
     return true;
 }
 

@@ -66,11 +66,12 @@ int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
 SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad) {
     SmemLayout L;
-    L.w = maxElem * 64;
-    L.contrib = L.w + maxElem * 16;
+    L.w = maxElem * 64;                                 // gradients: 4 float4 per element
+    L.contrib = L.w + round_up(maxElem * 8, 16);        // weights: float2 per element
     L.off = L.contrib + round_up(maxContribPad * 2, 16);
-    L.diag = L.off + maxOffPad * 8;
-    L.bar = L.diag + maxRowsPad * 8;
+    L.diag = L.off + maxOffPad * 16;
+    L.res = L.diag + maxRowsPad * 8;
+    L.bar = L.res + round_up(maxRowsPad * 48, 16);      // 12 floats per row
     L.bytes = L.bar + 16;
     return L;
 }
@@ -115,12 +116,14 @@ void build_tile_plan(Context &c) {
 
     std::vector<TileDesc> tiles;
     std::vector<int> tileElems;
-    std::vector<int2> offEnt, diagEnt;
+    std::vector<int4> offEnt;
+    std::vector<int2> diagEnt;
     std::vector<unsigned short> contrib;
     offEnt.reserve((size_t)nnz + N);
     diagEnt.reserve((size_t)N * 2);
     contrib.reserve((size_t)E * 16 + (size_t)N);
-    std::vector<int> mark(E, -1), local(E, 0), elems, rows, cnt, fill, start;
+    std::vector<int> mark(E, -1), local(E, 0), elems, rows, cnt, fill, start, keep;
+    std::vector<int> rowTile(N, -1), rowLocal(N, 0);
     int maxElem = 0, maxContrib = 0, maxOff = 0, maxRows = 0;
 
     int i = 0;
@@ -156,45 +159,67 @@ void build_tile_plan(Context &c) {
         T.diagBegin = (int)diagEnt.size();
         T.contribBegin = (int)contrib.size();
         T.nRows = (int)rows.size();
-        for (int r : rows) {
+        for (int k = 0; k < T.nRows; k++) {
+            rowTile[rows[k]] = tIndex;
+            rowLocal[rows[k]] = k;
+        }
+        for (int lr = 0; lr < T.nRows; lr++) {
+            const int r = rows[lr];
             const int b = rowPtr[r], len = rowPtr[r + 1] - b;
-            cnt.assign(len, 0);
-            auto where = [&](int cc) {
-                for (int m = 0; m < len; m++)
-                    if (col[b + m] == cc) return m;
+            auto where = [&](int row0, int rowLen, int cc) {
+                for (int m = 0; m < rowLen; m++)
+                    if (col[row0 + m] == cc) return m;
                 return -1;
             };
+            // which entries of the row this tile computes: the diagonal, entries to
+            // rows outside the tile, and (r, c) with c a later row of the tile,
+            // which also yields (c, r) transposed
+            keep.assign(len, 0);
+            for (int m = 0; m < len; m++) {
+                const int cc = col[b + m];
+                keep[m] = cc == r || rowTile[cc] != tIndex || rowLocal[cc] > lr;
+            }
+            cnt.assign(len, 0);
             for (int q = nptr[r]; q < nptr[r + 1]; q++) {
                 const int e = nelem[q] >> 2;
                 for (int k = 0; k < 4; k++) {
-                    const int m = where(e2n[4 * (size_t)e + k]);
+                    const int m = where(b, len, e2n[4 * (size_t)e + k]);
                     MFEM_REQUIRE(m >= 0, MFEM_ERR_PATTERN, "tile plan: pattern misses an element pair");
                     cnt[m]++;
                 }
             }
             start.assign(len + 1, 0);
-            for (int m = 0; m < len; m++) start[m + 1] = start[m] + cnt[m];
+            for (int m = 0; m < len; m++) start[m + 1] = start[m] + (keep[m] ? cnt[m] : 0);
             const int base = (int)contrib.size() - T.contribBegin;
             contrib.resize(contrib.size() + start[len]);
             fill.assign(len, 0);
             for (int q = nptr[r]; q < nptr[r + 1]; q++) {
                 const int e = nelem[q] >> 2, j = nelem[q] & 3;
                 for (int k = 0; k < 4; k++) {
-                    const int m = where(e2n[4 * (size_t)e + k]);
+                    const int m = where(b, len, e2n[4 * (size_t)e + k]);
+                    if (!keep[m]) continue;
                     contrib[T.contribBegin + base + start[m] + fill[m]++] =
                         (unsigned short)((local[e] << 4) | (j << 2) | k);
                 }
             }
             bool hasDiag = false;
             for (int m = 0; m < len; m++) {
+                if (!keep[m]) continue;
                 MFEM_REQUIRE(cnt[m] <= 255 && base + start[m] < (1 << 23), MFEM_ERR_CAPACITY,
                              "tile plan: too many contributions for one entry");
                 const int meta = ((base + start[m]) << 8) | cnt[m];
-                if (col[b + m] == r) {
+                const int cc = col[b + m];
+                if (cc == r) {
                     diagEnt.push_back(make_int2(r, meta));
                     hasDiag = true;
                 } else {
-                    offEnt.push_back(make_int2(b + m, meta));
+                    int tpos = -1;
+                    if (rowTile[cc] == tIndex) {
+                        const int tm = where(rowPtr[cc], rowPtr[cc + 1] - rowPtr[cc], r);
+                        MFEM_REQUIRE(tm >= 0, MFEM_ERR_PATTERN, "tile plan: pattern is not symmetric");
+                        tpos = rowPtr[cc] + tm;
+                    }
+                    offEnt.push_back(make_int4(b + m, tpos, meta, 0));
                 }
             }
             if (!hasDiag) diagEnt.push_back(make_int2(r, 0));
@@ -203,7 +228,6 @@ void build_tile_plan(Context &c) {
         T.nContrib = (int)contrib.size() - T.contribBegin;
         // pad every segment so that the next tile starts 16-byte aligned and
         // the bulk copies move whole 16-byte units that lie inside the arrays
-        while (offEnt.size() % 2) offEnt.push_back(make_int2(0, 0));
         while (diagEnt.size() % 2) diagEnt.push_back(make_int2(0, 0));
         while (contrib.size() % 8) contrib.push_back(0);
         T.nOffPad = (int)offEnt.size() - T.offBegin;
@@ -227,7 +251,7 @@ void build_tile_plan(Context &c) {
     };
     up(tp.desc, tiles.data(), tiles.size() * sizeof(TileDesc));
     up(tp.elems, tileElems.data(), tileElems.size() * 4);
-    up(tp.offEnt, offEnt.data(), offEnt.size() * sizeof(int2));
+    up(tp.offEnt, offEnt.data(), offEnt.size() * sizeof(int4));
     up(tp.diagEnt, diagEnt.data(), diagEnt.size() * sizeof(int2));
     up(tp.contrib, contrib.data(), contrib.size() * 2);
     MFEM_CUDA(cudaStreamSynchronize(c.stream));
@@ -239,7 +263,7 @@ TilePlanView plan_view(const TilePlan &tp) {
     TilePlanView P;
     P.desc = tp.desc.as<TileDesc>();
     P.elems = tp.elems.as<int>();
-    P.offEnt = tp.offEnt.as<int2>();
+    P.offEnt = tp.offEnt.as<int4>();
     P.diagEnt = tp.diagEnt.as<int2>();
     P.contrib = tp.contrib.as<unsigned short>();
     return P;

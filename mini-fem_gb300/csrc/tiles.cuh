@@ -13,7 +13,7 @@ constexpr int kTileThreads = 256;
 struct TileDesc {
     int diagBegin, nRows, nRowsPad;          // into diagEnt: (row, meta)
     int elemBegin, nElem;                    // into elems
-    int offBegin, nOff, nOffPad;             // into offEnt: (CSR position, meta)
+    int offBegin, nOff, nOffPad;             // into offEnt: (pos, transposed pos or -1, meta, 0)
     int contribBegin, nContrib, nContribPad; // into contrib (u16: local elem << 4 | j << 2 | k)
     int mesh;                                // batch: index of the mesh the tile belongs to
 };
@@ -23,7 +23,7 @@ struct TileDesc {
 struct TilePlanView {
     const TileDesc *desc;
     const int *elems;
-    const int2 *offEnt;
+    const int4 *offEnt;
     const int2 *diagEnt;
     const unsigned short *contrib;
 };
@@ -51,7 +51,7 @@ struct TileSets {
 
 // Byte offsets of the dynamic shared-memory regions.
 struct SmemLayout {
-    int w, contrib, off, diag, bar, bytes;
+    int w, contrib, off, diag, res, bar, bytes;
 };
 
 SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad);
