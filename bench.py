@@ -35,7 +35,7 @@ sys.path.insert(0, os.path.join(ROOT, "mini-fem_gb300"))
 
 import numpy as np  # noqa: E402
 
-N_SIDE = 100      # nodes per side of the benchmark cube (--n changes it for small cases)
+N_SIDE = 100      # nodes per side of the benchmark cube (--side changes it for small cases)
 SEED = 2024
 WORKLOAD = "ela_cube100_5.8M_tets"
 METRIC = "ela assembly Melem/s @5.8M tets: FP32-batched vs FP64-plain; % HBM roofline"
@@ -361,10 +361,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-iters", type=int, default=3)
-    ap.add_argument("--n", type=int, default=N_SIDE,
+    ap.add_argument("--side", type=int, default=N_SIDE,
                     help="nodes per cube side (100 = the benchmark mesh; smaller for profiling)")
     args = ap.parse_args()
-    globals()["N_SIDE"] = args.n
+    globals()["N_SIDE"] = args.side
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
 

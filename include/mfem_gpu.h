@@ -132,7 +132,10 @@ int mfem_get_flagged(mfem_context *ctx, int *nbFlagged);
 /* Tuning knobs (no counterpart in the reference): "sliver_threshold" (as above),
  * "fp32_kernel" (0: per-element gradient records + one thread per entry,
  * 1: spatial row tiles with gradients in shared memory, the default),
- * "tile_rows" / "tile_elems" (tile size limits of kernel 1). */
+ * "tile_rows" / "tile_elems" (tile size limits of kernel 1), "wait_limit" (polls
+ * of the kernel's bounded wait for its staged copies before it gives up and the
+ * next result read returns MFEM_ERR_TIMEOUT) and "test_missing_bytes" (testing
+ * the bounded wait only: the wait expects that many bytes more than arrive). */
 int mfem_set_option(mfem_context *ctx, const char *name, double value);
 
 /* ---- results ---------------------------------------------------------------- */

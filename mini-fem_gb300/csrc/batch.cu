@@ -69,7 +69,7 @@ template <bool PREC>
 __global__ void __launch_bounds__(kTileThreads)
 k_batch_tile32(const BatchMesh *__restrict__ meshes, const TileDesc *__restrict__ desc,
                const int *__restrict__ order, int nWork, SmemLayout L, float qthr2, int *counters,
-               int *workCounter) {
+               int *workCounter, TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ int sWork;
     for (;;) {
@@ -82,9 +82,9 @@ k_batch_tile32(const BatchMesh *__restrict__ meshes, const TileDesc *__restrict_
         const BatchMesh &B = meshes[T.mesh];
         bool ok;
         if (B.op == MFEM_OP_LAP)
-            ok = tilek::tile_body<MFEM_OP_LAP, PREC>(T, B.geo, B.sets, B.plan, L, qthr2, sm, counters);
+            ok = tilek::tile_body<MFEM_OP_LAP, PREC>(T, B.geo, B.sets, B.plan, L, qthr2, sm, counters, ctl);
         else
-            ok = tilek::tile_body<MFEM_OP_ELA, PREC>(T, B.geo, B.sets, B.plan, L, qthr2, sm, counters);
+            ok = tilek::tile_body<MFEM_OP_ELA, PREC>(T, B.geo, B.sets, B.plan, L, qthr2, sm, counters, ctl);
         if (!ok) return;
         __syncthreads();   // shared memory is reused by the next item
     }
@@ -212,10 +212,10 @@ void record32(mfem_batch &b, bool withPrec) {
     const float q = b.items[0]->ctx->c.sliverThreshold;
     if (withPrec)
         k_batch_tile32<true><<<b.gridPersistent, kTileThreads, b.layout.bytes, b.stream>>>(
-            tab, b.desc.as<TileDesc>(), b.order.as<int>(), b.nWork, b.layout, q * q, cnt, cnt + 4);
+            tab, b.desc.as<TileDesc>(), b.order.as<int>(), b.nWork, b.layout, q * q, cnt, cnt + 4, TileCtl{1u << 22, 0u});
     else
         k_batch_tile32<false><<<b.gridPersistent, kTileThreads, b.layout.bytes, b.stream>>>(
-            tab, b.desc.as<TileDesc>(), b.order.as<int>(), b.nWork, b.layout, q * q, cnt, cnt + 4);
+            tab, b.desc.as<TileDesc>(), b.order.as<int>(), b.nWork, b.layout, q * q, cnt, cnt + 4, TileCtl{1u << 22, 0u});
     check_launch("k_batch_tile32");
 }
 

@@ -126,6 +126,19 @@ void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int n
     c.hostE2n = e2n;
 }
 
+// Errors kernels report through the status words after they were enqueued:
+// status[6] = a bounded wait gave up.
+void check_async(Context &c) {
+    int h[8];
+    read_status(c, h, 8);
+    if (h[6]) {
+        MFEM_CUDA(cudaMemsetAsync(status_ptr(c) + 6, 0, sizeof(int), c.stream));
+        MFEM_CUDA(cudaStreamSynchronize(c.stream));
+        throw Error(MFEM_ERR_TIMEOUT, "a device wait gave up (staged copies did not arrive in time); "
+                                      "the results of that call are incomplete");
+    }
+}
+
 void upload_coords(Context &c, const double *coord) {
     MFEM_REQUIRE(coord, MFEM_ERR_INVALID_ARG, "null coord");
     MFEM_CUDA(cudaMemcpyAsync(c.coord.as<double>(), coord, sizeof(double) * 3 * (size_t)c.nbNodes,
@@ -403,6 +416,13 @@ int mfem_set_option(mfem_context *ctx, const char *name, double value) {
             MFEM_REQUIRE(value >= 1 && value <= 1024, MFEM_ERR_INVALID_ARG, "tile_rows in [1, 1024]");
             c.tiles.maxRows = (int)value;
             c.tiles.built = false;
+        } else if (n == "wait_limit") {
+            MFEM_REQUIRE(value >= 1 && value <= 4294967295.0, MFEM_ERR_INVALID_ARG, "wait_limit >= 1");
+            c.waitLimit = (unsigned)value;
+        } else if (n == "test_missing_bytes") {
+            MFEM_REQUIRE(value >= 0 && value <= 4096 && (long long)value % 16 == 0, MFEM_ERR_INVALID_ARG,
+                         "test_missing_bytes: a multiple of 16 in [0, 4096]");
+            c.testExtraTx = (unsigned)value;
         } else if (n == "tile_elems") {
             MFEM_REQUIRE(value >= 64 && value <= 4096, MFEM_ERR_INVALID_ARG, "tile_elems in [64, 4096]");
             c.tiles.maxElem = (int)value;
@@ -424,6 +444,7 @@ int mfem_get_flagged(mfem_context *ctx, int *nbFlagged) {
 
 int mfem_get_values(mfem_context *ctx, double *values) {
     return mfem::guarded(ctx, [&](Context &c) {
+        mfem::check_async(c);
         MFEM_REQUIRE(c.lastOp >= 0, MFEM_ERR_STATE, "nothing assembled");
         MFEM_REQUIRE(values, MFEM_ERR_INVALID_ARG, "null values");
         const long long n = (long long)c.nnz * mfem::op_dim(c.lastOp);
@@ -442,6 +463,7 @@ int mfem_get_values(mfem_context *ctx, double *values) {
 
 int mfem_get_values_f32(mfem_context *ctx, float *values) {
     return mfem::guarded(ctx, [&](Context &c) {
+        mfem::check_async(c);
         MFEM_REQUIRE(c.lastOp >= 0 && c.lastPrecision == MFEM_FP32, MFEM_ERR_STATE,
                      "no FP32 assembly to read");
         MFEM_REQUIRE(values, MFEM_ERR_INVALID_ARG, "null values");
@@ -454,6 +476,7 @@ int mfem_get_values_f32(mfem_context *ctx, float *values) {
 
 int mfem_get_prec(mfem_context *ctx, double *prec) {
     return mfem::guarded(ctx, [&](Context &c) {
+        mfem::check_async(c);
         MFEM_REQUIRE(c.lastOp >= 0 && c.prec.ptr, MFEM_ERR_STATE, "no preconditioner");
         MFEM_REQUIRE(prec, MFEM_ERR_INVALID_ARG, "null prec");
         MFEM_CUDA(cudaMemcpyAsync(prec, c.prec.as<double>(),
@@ -479,7 +502,7 @@ int mfem_prec_device(mfem_context *ctx, double **prec) {
 }
 
 int mfem_synchronize(mfem_context *ctx) {
-    return mfem::guarded(ctx, [&](Context &c) { MFEM_CUDA(cudaStreamSynchronize(c.stream)); });
+    return mfem::guarded(ctx, [&](Context &c) { mfem::check_async(c); });
 }
 
 int mfem_profile(mfem_context *ctx, int enable) {

@@ -106,6 +106,9 @@ struct Context {
     // kept in status[5].
     float sliverThreshold = 0.1f;
     bool flaggedPending = false;
+    // bounded device waits (tile kernel): polls before giving up, and bytes the
+    // barrier expects on top of the real copies (testing the limit only)
+    unsigned waitLimit = 1u << 22, testExtraTx = 0;
 
     // scratch
     DevBuf grad;                      // per-element gradient records

@@ -135,7 +135,7 @@ __device__ __forceinline__ bool inv3_sym(double d[6]) {
 template <int OP, bool PREC>
 __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, const TileSets &S,
                                           const TilePlanView &P, const SmemLayout &L, float qthr2,
-                                          unsigned char *sm, int *counters) {
+                                          unsigned char *sm, int *counters, TileCtl ctl) {
     float4 *G = reinterpret_cast<float4 *>(sm);                       // 4 per element
     float2 *W = reinterpret_cast<float2 *>(sm + L.w);                 // (B, mu) or (kappa, -)
     unsigned short *sC = reinterpret_cast<unsigned short *>(sm + L.contrib);
@@ -153,7 +153,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const unsigned bc = (unsigned)T.nContribPad * 2u, bo = (unsigned)T.nOffPad * 16u,
                        bd = (unsigned)T.nRowsPad * 8u;
-        mbar_expect_tx(bar, bc + bo + bd);
+        mbar_expect_tx(bar, bc + bo + bd + ctl.extraTx);
         if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar);
         if (bo) bulk_g2s(sOff, P.offEnt + T.offBegin, bo, bar);
         if (bd) bulk_g2s(sDiag, P.diagEnt + T.diagBegin, bd, bar);
@@ -174,7 +174,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
 
     // bounded wait for the staged segments (the CTA agrees on the outcome)
     bool ok = false;
-    for (int it = 0; it < (1 << 22) && !ok; it++) ok = mbar_try_wait(bar, 0);
+    for (unsigned it = 0; it < ctl.waitLimit && !ok; it++) ok = mbar_try_wait(bar, 0);
     if (__syncthreads_or(!ok)) {
         if (tid == 0) atomicOr(counters + 2, 1);
         return false;

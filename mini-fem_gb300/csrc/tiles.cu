@@ -34,10 +34,11 @@ namespace {
 
 template <int OP, bool PREC>
 __global__ void __launch_bounds__(kTileThreads)
-k_tile32(TilePlanView P, TileMesh M, TileSets S, SmemLayout L, float qthr2, int *counters) {
+k_tile32(TilePlanView P, TileMesh M, TileSets S, SmemLayout L, float qthr2, int *counters,
+         TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char sm[];
     const TileDesc T = P.desc[blockIdx.x];
-    tilek::tile_body<OP, PREC>(T, M, S, P, L, qthr2, sm, counters);
+    tilek::tile_body<OP, PREC>(T, M, S, P, L, qthr2, sm, counters, ctl);
 }
 
 __global__ void k_split_coords_t(const double *__restrict__ coord, int nbNodes,
@@ -309,7 +310,8 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     c.timer.begin(fusePrec ? "tile32+prec" : "tile32", c.stream);
     auto launch = [&](auto kern) {
         MFEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
-        kern<<<tp.nTiles, kTileThreads, L.bytes, c.stream>>>(P, M, S, L, q * q, st + 4);
+        kern<<<tp.nTiles, kTileThreads, L.bytes, c.stream>>>(P, M, S, L, q * q, st + 4,
+                                                             TileCtl{c.waitLimit, c.testExtraTx});
     };
     if (op == MFEM_OP_LAP) {
         if (fusePrec) launch(k_tile32<MFEM_OP_LAP, true>);

@@ -49,6 +49,14 @@ struct TileSets {
     int nSets;
 };
 
+// Bounded-wait control of the tile kernel: the staged-copy wait gives up after
+// waitLimit polls and flags MFEM_ERR_TIMEOUT; extraTx (testing only) makes the
+// barrier expect bytes that never arrive, so that the limit is exercised.
+struct TileCtl {
+    unsigned waitLimit;
+    unsigned extraTx;
+};
+
 // Byte offsets of the dynamic shared-memory regions.
 struct SmemLayout {
     int w, contrib, off, diag, res, bar, bytes;
