@@ -137,6 +137,11 @@ int mfem_get_flagged(mfem_context *ctx, int *nbFlagged);
  * next result read returns MFEM_ERR_TIMEOUT) and "test_missing_bytes" (testing
  * the bounded wait only: the wait expects that many bytes more than arrive). */
 int mfem_set_option(mfem_context *ctx, const char *name, double value);
+/* Statistics of the FP32 tile plan (built on demand): tiles, elements over all
+ * tiles (halo included), off-diagonal units, contributions, shared memory per
+ * CTA in bytes. */
+int mfem_tile_info(mfem_context *ctx, int *nbTiles, long long *nbTileElems,
+                   long long *nbUnits, long long *nbContrib, int *smemBytes);
 
 /* ---- results ---------------------------------------------------------------- */
 int mfem_get_values(mfem_context *ctx, double *values);     /* nbEdges*opDim, FP64 */

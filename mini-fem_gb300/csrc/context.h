@@ -34,6 +34,8 @@ struct TilePlan {
     int maxRows = 48, maxElem = 512;
     int nTiles = 0;
     long long nTileElems = 0;   // sum over tiles of their element counts
+    long long nUnits = 0;       // off-diagonal units (an intra-tile pair counts once)
+    long long nContrib = 0;     // contributions summed per coefficient set
     SmemLayout layout{};
     DevBuf desc, elems, offEnt, diagEnt, contrib;
 };

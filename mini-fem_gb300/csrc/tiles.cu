@@ -257,6 +257,12 @@ void build_tile_plan(Context &c) {
     up(tp.contrib, contrib.data(), contrib.size() * 2);
     MFEM_CUDA(cudaStreamSynchronize(c.stream));
     tp.nTileElems = (long long)tileElems.size();
+    tp.nUnits = 0;
+    tp.nContrib = 0;
+    for (const TileDesc &T : tiles) {
+        tp.nUnits += T.nOff;
+        tp.nContrib += T.nContrib;
+    }
     tp.built = true;
 }
 
@@ -329,3 +335,23 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
 }
 
 }  // namespace mfem
+
+extern "C" int mfem_tile_info(mfem_context *ctx, int *nbTiles, long long *nbTileElems,
+                              long long *nbUnits, long long *nbContrib, int *smemBytes) {
+    if (!ctx) return MFEM_ERR_INVALID_ARG;
+    try {
+        MFEM_CUDA(cudaSetDevice(ctx->c.device));
+        MFEM_REQUIRE(ctx->c.hasPattern, MFEM_ERR_STATE, "no CSR pattern");
+        mfem::build_tile_plan(ctx->c);
+        const mfem::TilePlan &tp = ctx->c.tiles;
+        if (nbTiles) *nbTiles = tp.nTiles;
+        if (nbTileElems) *nbTileElems = tp.nTileElems;
+        if (nbUnits) *nbUnits = tp.nUnits;
+        if (nbContrib) *nbContrib = tp.nContrib;
+        if (smemBytes) *smemBytes = tp.layout.bytes;
+        return MFEM_OK;
+    } catch (const mfem::Error &e) {
+        ctx->c.lastError = e.what();
+        return e.code;
+    }
+}

@@ -45,6 +45,8 @@ _SIGS = {
     "mfem_prec_inversion": ([_vp, _ip], C.c_int),
     "mfem_set_sliver_threshold": ([_vp, C.c_double], C.c_int),
     "mfem_set_option": ([_vp, C.c_char_p, C.c_double], C.c_int),
+    "mfem_tile_info": ([_vp, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                        C.POINTER(C.c_longlong), _ip], C.c_int),
     "mfem_get_flagged": ([_vp, _ip], C.c_int),
     "mfem_get_values": ([_vp, _vp], C.c_int),
     "mfem_get_values_f32": ([_vp, _vp], C.c_int),

@@ -162,6 +162,14 @@ class Assembler:
     def set_option(self, name: str, value: float):
         self._check(N.lib.mfem_set_option(self._h, name.encode(), float(value)))
 
+    def tile_info(self) -> dict:
+        t, s = C.c_int(), C.c_int()
+        e, u, k = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        self._check(N.lib.mfem_tile_info(self._h, C.byref(t), C.byref(e), C.byref(u), C.byref(k),
+                                         C.byref(s)))
+        return {"tiles": t.value, "tile_elems": e.value, "units": u.value,
+                "contributions": k.value, "smem_bytes": s.value}
+
     def flagged(self) -> int:
         n = C.c_int()
         self._check(N.lib.mfem_get_flagged(self._h, C.byref(n)))

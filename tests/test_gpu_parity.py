@@ -358,7 +358,7 @@ def test_bounded_wait_reports_timeout_and_context_stays_usable(gpu):
     m = cube_mesh(4, seed=2, op="ela")
     a = gpu(0)
     a.set_mesh(m.coord, m.elemToNode)
-    a.create_nodeToNode("sorted")
+    a.create_nodeToNode("reference")
     a.set_coefficients("ela", m.coef)
     a.set_option("wait_limit", 200)
     a.set_option("test_missing_bytes", 16)
