@@ -42,6 +42,7 @@ struct mfem_batch {
         mfem_context *ctx;
         int op, nSets;
         mfem::DevBuf coef;            // nSets x per-element coefficients (empty: constants)
+        mfem::DevBuf w32;             // nSets x per-element FP32 weights
         bool hasCoef = false;
         size_t valOff = 0, precOff = 0, nodeOff = 0;
     };
@@ -66,7 +67,7 @@ namespace mfem {
 namespace {
 
 template <bool PREC>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, 4)
 k_batch_tile32(const BatchMesh *__restrict__ meshes, const TileDesc *__restrict__ desc,
                const int *__restrict__ order, int nWork, SmemLayout L, float qthr2, int *counters,
                int *workCounter, TileCtl ctl) {
@@ -165,8 +166,8 @@ void prepare(mfem_batch &b) {
         B.geo.e2n = c.e2n.as<int4>();
         B.geo.diagPos = c.diagPos.as<int>();
         B.geo.mask = c.hasMask ? c.mask.as<unsigned char>() : nullptr;
-        B.sets.coef = it->hasCoef ? it->coef.as<double>() : nullptr;
-        B.sets.coefStride = (size_t)c.nbElem * (it->op == MFEM_OP_LAP ? 1 : 2);
+        B.sets.w = (const float2 *)it->w32.reserve(sizeof(float2) * (size_t)c.nbElem * it->nSets);
+        B.sets.wStride = (size_t)c.nbElem;
         B.sets.values = nullptr;          // filled per precision below
         B.sets.valuesStride = (size_t)c.nnz * op_dim(it->op);
         B.sets.prec = b.prec.as<double>() + it->precOff;
@@ -204,6 +205,9 @@ void record32(mfem_batch &b, bool withPrec) {
     for (auto *it : b.items) {
         Context &c = it->ctx->c;
         split_coords(c, hi + it->nodeOff, hi + b.totalNodes + it->nodeOff, b.stream);
+        const long long n = (long long)c.nbElem * (it->hasCoef ? it->nSets : 1);
+        weights32_all(it->op, it->hasCoef ? it->coef.as<double>() : nullptr, n, it->w32.as<float2>(),
+                      b.stream);
     }
     int *cnt = b.counters.as<int>();
     MFEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * 8, b.stream));

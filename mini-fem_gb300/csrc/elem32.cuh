@@ -19,19 +19,30 @@ __device__ __forceinline__ float diff_prod(float a, float b, float c, float d) {
     return f + e;
 }
 
-// Gradients g[4][3] of one element in FP32.  Returns true when the element was
-// flagged (quality |6V| / (|a||b||c|) below sqrt(qthr2)) and computed in FP64.
-__device__ __forceinline__ bool grad32(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
-                                       const double *__restrict__ coord, int4 nd, float qthr2,
-                                       float g[12]) {
-    const float4 h0 = hi[nd.x], h1 = hi[nd.y], h2 = hi[nd.z], h3 = hi[nd.w];
-    const float4 l0 = lo[nd.x], l1 = lo[nd.y], l2 = lo[nd.z], l3 = lo[nd.w];
-    const float xa = (h0.x - h3.x) + (l0.x - l3.x), ya = (h0.y - h3.y) + (l0.y - l3.y),
-                za = (h0.z - h3.z) + (l0.z - l3.z);
-    const float xb = (h2.x - h3.x) + (l2.x - l3.x), yb = (h2.y - h3.y) + (l2.y - l3.y),
-                zb = (h2.z - h3.z) + (l2.z - l3.z);
-    const float xc = (h1.x - h3.x) + (l1.x - l3.x), yc = (h1.y - h3.y) + (l1.y - l3.y),
-                zc = (h1.z - h3.z) + (l1.z - l3.z);
+// The eight coordinate words (hi and lo of the four nodes) of one element.
+struct ElemCoords {
+    float4 h0, h1, h2, h3, l0, l1, l2, l3;
+};
+
+__device__ __forceinline__ ElemCoords load_coords(const float4 *__restrict__ hi,
+                                                  const float4 *__restrict__ lo, int4 nd) {
+    ElemCoords c;
+    c.h0 = hi[nd.x]; c.h1 = hi[nd.y]; c.h2 = hi[nd.z]; c.h3 = hi[nd.w];
+    c.l0 = lo[nd.x]; c.l1 = lo[nd.y]; c.l2 = lo[nd.z]; c.l3 = lo[nd.w];
+    return c;
+}
+
+// Gradients g[4][3] of one element in FP32 from its loaded coordinates.
+// Returns true when the element was flagged (quality |6V| / (|a||b||c|) below
+// sqrt(qthr2)) and computed in FP64 from `coord` instead.
+__device__ __forceinline__ bool grad32_from(const ElemCoords &C, const double *__restrict__ coord,
+                                            int4 nd, float qthr2, float g[12]) {
+    const float xa = (C.h0.x - C.h3.x) + (C.l0.x - C.l3.x), ya = (C.h0.y - C.h3.y) + (C.l0.y - C.l3.y),
+                za = (C.h0.z - C.h3.z) + (C.l0.z - C.l3.z);
+    const float xb = (C.h2.x - C.h3.x) + (C.l2.x - C.l3.x), yb = (C.h2.y - C.h3.y) + (C.l2.y - C.l3.y),
+                zb = (C.h2.z - C.h3.z) + (C.l2.z - C.l3.z);
+    const float xc = (C.h1.x - C.h3.x) + (C.l1.x - C.l3.x), yc = (C.h1.y - C.h3.y) + (C.l1.y - C.l3.y),
+                zc = (C.h1.z - C.h3.z) + (C.l1.z - C.l3.z);
     g[0] = diff_prod(yb, zc, yc, zb); g[1] = diff_prod(zb, xc, zc, xb); g[2] = diff_prod(xb, yc, xc, yb);
     g[3] = diff_prod(ya, zb, yb, za); g[4] = diff_prod(za, xb, zb, xa); g[5] = diff_prod(xa, yb, xb, ya);
     g[6] = diff_prod(yc, za, ya, zc); g[7] = diff_prod(zc, xa, za, xc); g[8] = diff_prod(xc, ya, xa, yc);
@@ -53,6 +64,12 @@ __device__ __forceinline__ bool grad32(const float4 *__restrict__ hi, const floa
 #pragma unroll
     for (int i = 0; i < 12; i++) g[i] *= r;
     return false;
+}
+
+__device__ __forceinline__ bool grad32(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                       const double *__restrict__ coord, int4 nd, float qthr2,
+                                       float g[12]) {
+    return grad32_from(load_coords(hi, lo, nd), coord, nd, qthr2, g);
 }
 
 // double -> float, round to nearest even, with integer operations so that it

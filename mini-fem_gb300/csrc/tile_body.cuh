@@ -11,6 +11,10 @@
 namespace mfem {
 namespace tilek {
 
+// Phase 1 loads two elements per thread before computing either (more loads in
+// flight per thread, more registers).
+constexpr bool kPairLoads = true;
+
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
@@ -159,15 +163,42 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         if (bd) bulk_g2s(sDiag, P.diagEnt + T.diagBegin, bd, bar);
     }
 
-    // 1. gradients of the tile's elements (and the weights of set 0)
+    // 1. gradients of the tile's elements (and the weights of set 0); with
+    //    kPairLoads two elements per thread per pass, all their loads issued first
     int flagged = 0;
-    for (int i = tid; i < T.nElem; i += kTileThreads) {
-        const int e = P.elems[T.elemBegin + i];
-        float g[12];
-        flagged += grad32(M.hi, M.lo, M.coord, M.e2n[e], qthr2, g);
+    if constexpr (kPairLoads) {
+        for (int i0 = tid; i0 < T.nElem; i0 += 2 * kTileThreads) {
+            const int i1 = i0 + kTileThreads;
+            const bool has1 = i1 < T.nElem;
+            const int4 n0 = P.conn[T.elemBegin + i0];
+            const int4 n1 = has1 ? P.conn[T.elemBegin + i1] : n0;
+            const int e0 = P.elems[T.elemBegin + i0];
+            const int e1 = has1 ? P.elems[T.elemBegin + i1] : e0;
+            const ElemCoords c0 = load_coords(M.hi, M.lo, n0);
+            const ElemCoords c1 = load_coords(M.hi, M.lo, n1);
+            const float2 w0 = S.w[e0], w1 = S.w[e1];
+            float g[12];
+            flagged += grad32_from(c0, M.coord, n0, qthr2, g);
 #pragma unroll
-        for (int j = 0; j < 4; j++) G[4 * i + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
-        W[i] = weights32<OP>(S.coef, e);
+            for (int j = 0; j < 4; j++) G[4 * i0 + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
+            W[i0] = w0;
+            if (has1) {
+                flagged += grad32_from(c1, M.coord, n1, qthr2, g);
+#pragma unroll
+                for (int j = 0; j < 4; j++) G[4 * i1 + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
+                W[i1] = w1;
+            }
+        }
+    } else {
+        for (int i = tid; i < T.nElem; i += kTileThreads) {
+            const int4 nd = P.conn[T.elemBegin + i];
+            const float2 w = S.w[P.elems[T.elemBegin + i]];
+            float g[12];
+            flagged += grad32(M.hi, M.lo, M.coord, nd, qthr2, g);
+#pragma unroll
+            for (int j = 0; j < 4; j++) G[4 * i + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
+            W[i] = w;
+        }
     }
     if (flagged) atomicAdd(counters + 1, flagged);
     __syncthreads();
@@ -187,9 +218,8 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         if (set > 0) {
             // weights of this set (every thread is done with the previous set's)
             __syncthreads();
-            const double *coef = S.coef ? S.coef + (size_t)set * S.coefStride : nullptr;
-            for (int i = tid; i < T.nElem; i += kTileThreads)
-                W[i] = weights32<OP>(coef, P.elems[T.elemBegin + i]);
+            const float2 *w = S.w + (size_t)set * S.wStride;
+            for (int i = tid; i < T.nElem; i += kTileThreads) W[i] = w[P.elems[T.elemBegin + i]];
             __syncthreads();
         }
 

@@ -33,12 +33,20 @@ namespace mfem {
 namespace {
 
 template <int OP, bool PREC>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, 4)
 k_tile32(TilePlanView P, TileMesh M, TileSets S, SmemLayout L, float qthr2, int *counters,
          TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char sm[];
     const TileDesc T = P.desc[blockIdx.x];
     tilek::tile_body<OP, PREC>(T, M, S, P, L, qthr2, sm, counters, ctl);
+}
+
+// Per-element weights of the FP32 blocks for n = E * nSets elements (sets laid
+// out one after the other, as the coefficient arrays are).
+template <int OP>
+__global__ void k_weights32(const double *__restrict__ coef, long long n, float2 *__restrict__ w) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) w[i] = weights32<OP>(coef, (int)i);
 }
 
 __global__ void k_split_coords_t(const double *__restrict__ coord, int nbNodes,
@@ -252,6 +260,14 @@ void build_tile_plan(Context &c) {
     };
     up(tp.desc, tiles.data(), tiles.size() * sizeof(TileDesc));
     up(tp.elems, tileElems.data(), tileElems.size() * 4);
+    {
+        std::vector<int4> conn(tileElems.size());
+        for (size_t k = 0; k < tileElems.size(); k++) {
+            const size_t e = (size_t)tileElems[k];
+            conn[k] = make_int4(e2n[4 * e], e2n[4 * e + 1], e2n[4 * e + 2], e2n[4 * e + 3]);
+        }
+        up(tp.conn, conn.data(), conn.size() * sizeof(int4));
+    }
     up(tp.offEnt, offEnt.data(), offEnt.size() * sizeof(int4));
     up(tp.diagEnt, diagEnt.data(), diagEnt.size() * sizeof(int2));
     up(tp.contrib, contrib.data(), contrib.size() * 2);
@@ -270,10 +286,17 @@ TilePlanView plan_view(const TilePlan &tp) {
     TilePlanView P;
     P.desc = tp.desc.as<TileDesc>();
     P.elems = tp.elems.as<int>();
+    P.conn = tp.conn.as<int4>();
     P.offEnt = tp.offEnt.as<int4>();
     P.diagEnt = tp.diagEnt.as<int2>();
     P.contrib = tp.contrib.as<unsigned short>();
     return P;
+}
+
+void weights32_all(int op, const double *coef, long long n, float2 *w, cudaStream_t s) {
+    if (op == MFEM_OP_LAP) k_weights32<MFEM_OP_LAP><<<blocks_for(n, 256), 256, 0, s>>>(coef, n, w);
+    else k_weights32<MFEM_OP_ELA><<<blocks_for(n, 256), 256, 0, s>>>(coef, n, w);
+    check_launch("k_weights32");
 }
 
 void split_coords(const Context &c, float4 *hi, float4 *lo, cudaStream_t s) {
@@ -290,8 +313,10 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     double *prec = fusePrec ? (double *)c.prec.reserve(sizeof(double) * (size_t)N * dim) : nullptr;
     float4 *hi = (float4 *)c.scratch.reserve(sizeof(float4) * 2 * (size_t)N);
     float4 *lo = hi + N;
-    c.timer.begin("split_coords", c.stream);
+    float2 *w = (float2 *)c.tiles.w32.reserve(sizeof(float2) * (size_t)c.nbElem);
+    c.timer.begin("split_coords+weights", c.stream);
     split_coords(c, hi, lo, c.stream);
+    weights32_all(op, c.coefOp == op ? c.coef.as<double>() : nullptr, c.nbElem, w, c.stream);
     c.timer.end(c.stream);
     int *st = status_ptr(c);
     MFEM_CUDA(cudaMemsetAsync(st + 4, 0, sizeof(int) * 3, c.stream));
@@ -303,8 +328,8 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     M.diagPos = c.diagPos.as<int>();
     M.mask = c.hasMask ? c.mask.as<unsigned char>() : nullptr;
     TileSets S;
-    S.coef = c.coefOp == op ? c.coef.as<double>() : nullptr;
-    S.coefStride = 0;
+    S.w = w;
+    S.wStride = 0;
     S.values = c.values.as<float>();
     S.valuesStride = 0;
     S.prec = prec;

@@ -22,7 +22,8 @@ struct TileDesc {
 
 struct TilePlanView {
     const TileDesc *desc;
-    const int *elems;
+    const int *elems;            // element ids of each tile (ascending)
+    const int4 *conn;            // their 0-based nodes, in the same order
     const int4 *offEnt;
     const int2 *diagEnt;
     const unsigned short *contrib;
@@ -37,11 +38,13 @@ struct TileMesh {
     const unsigned char *mask;   // Dirichlet bits per node, or NULL
 };
 
-// Coefficient sets of one mesh and where their results go: set s reads
-// coef + s*coefStride and writes values + s*valuesStride, prec + s*precStride.
+// Coefficient sets of one mesh and where their results go: set s reads the
+// per-element weights w + s*wStride ((B, mu) for ela, (kappa, 0) for lap, made
+// by k_weights32 from the FP64 coefficients) and writes values + s*valuesStride,
+// prec + s*precStride.
 struct TileSets {
-    const double *coef;          // per-element kappa or (E, nu); NULL: reference constants
-    size_t coefStride;
+    const float2 *w;
+    size_t wStride;
     float *values;
     size_t valuesStride;
     double *prec;                // NULL: no preconditioner
