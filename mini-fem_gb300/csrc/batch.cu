@@ -67,7 +67,7 @@ namespace mfem {
 namespace {
 
 template <bool PREC>
-__global__ void __launch_bounds__(kTileThreads, 4)
+__global__ void __launch_bounds__(kTileThreads)
 k_batch_tile32(const BatchMesh *__restrict__ meshes, const TileDesc *__restrict__ desc,
                const int *__restrict__ order, int nWork, SmemLayout L, float qthr2, int *counters,
                int *workCounter, TileCtl ctl) {

@@ -11,9 +11,10 @@
 namespace mfem {
 namespace tilek {
 
-// Phase 1 loads two elements per thread before computing either (more loads in
-// flight per thread, more registers).
-constexpr bool kPairLoads = true;
+// Phase 1 can load two elements per thread before computing either (more loads
+// in flight per thread, more registers); measured slower on the 100^3 cube
+// (0.99 vs 0.90 ms), so one element per pass.
+constexpr bool kPairLoads = false;
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));

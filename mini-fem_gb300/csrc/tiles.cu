@@ -33,7 +33,7 @@ namespace mfem {
 namespace {
 
 template <int OP, bool PREC>
-__global__ void __launch_bounds__(kTileThreads, 4)
+__global__ void __launch_bounds__(kTileThreads)
 k_tile32(TilePlanView P, TileMesh M, TileSets S, SmemLayout L, float qthr2, int *counters,
          TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char sm[];
