@@ -235,6 +235,42 @@ def run_ours(args, rank, world, local_rank):
         prof[prec] = {k: sum(v) / len(v) for k, v in agg.items()}
     flagged = a.flagged()
 
+    # accuracy of the FP32 step against the FP64 one (the FP64 gather equals the
+    # oracle bit for bit), untimed
+    from minifem import metrics
+    a.assembly("ela", "fp64", "gather", prec=True)
+    v64, p64 = a.values(), a.prec()
+    a.assembly("ela", "fp32", "gather", prec=True)
+    v32, p32 = a.values(), a.prec()
+    errors = metrics.entry_errors(row, col, v64, v32, 9)
+    errors["preconditioned_operator_rel"] = metrics.operator_error(row, col, v64, p64, v32, p32, 9)
+    del v64, p64, v32, p32
+
+    # FP32 after reverse Cuthill-McKee renumbering of the nodes
+    from minifem.meshgen import renumber_nodes
+    rmesh = renumber_nodes(mesh, a.rcm_permutation())
+    ar = minifem.Assembler(local_rank)
+    ar.set_mesh(rmesh.coord, rmesh.elemToNode)
+    ar.create_nodeToNode("sorted")
+    ar.set_coefficients("ela", rmesh.coef)
+    ar.set_check_bounds(O.checkbounds(rmesh.boundNodesCode))
+    rstream = torch.cuda.ExternalStream(ar.stream)
+    for _ in range(args.warmup):
+        ar.assembly("ela", "fp32", "gather", prec=True)
+    rms = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(rstream):
+            flush.fill_(1.0)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(rstream)
+        ar.assembly("ela", "fp32", "gather", prec=True)
+        with torch.cuda.stream(rstream):
+            e.record(rstream)
+        rms.append((s, e))
+    torch.cuda.synchronize()
+    t_rcm = statistics.mean(x.elapsed_time(y) for x, y in rms)
+    ar.close()
+
     # maximum over ranks
     t32 = statistics.mean(ms32)
     t64 = statistics.mean(ms64)
@@ -283,6 +319,9 @@ def run_ours(args, rank, world, local_rank):
         "fp64_plain": {"value": round(melem(t64), 1), "unit": "Melem/s", "ms_per_step": round(t64, 4),
                        "bit_exact": "gather, -fmad=false", "roofline": r64, "step_roofline": s64},
         "fp32_over_fp64": round(t64 / t32, 2),
+        "fp32_errors_vs_fp64": errors,
+        "fp32_rcm": {"value": round(melem(t_rcm), 1), "unit": "Melem/s", "ms_per_step": round(t_rcm, 4),
+                     "renumbering": "reverse Cuthill-McKee (mfem_rcm_permutation)"},
         "kernels_ms": prof,
         "flagged_slivers": flagged,
         "e2e": {"value": round(melem(te2e), 1), "unit": "Melem/s", "ms_per_step": round(te2e, 4),
@@ -353,6 +392,155 @@ def run_reference(args, rank, world):
             "e2e": {"value": v, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---- supplementary workloads (--workload): the other benchmark configurations ----
+
+def _timer(torch, stream, flush):
+    def run(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                e.record(stream)
+            evs.append((s, e))
+        torch.cuda.synchronize()
+        return statistics.mean(x.elapsed_time(y) for x, y in evs)
+    return run
+
+
+def run_cube30(args, op):
+    """30^3 cube (146,334 tets), lap or ela: FP64 gather (bit-exact), colour scatter,
+    atomics and FP32, with the oracle port timed beside them."""
+    import torch
+    import minifem
+    import pyoracle as O
+    from minifem.meshgen import cube_mesh
+    mesh = cube_mesh(30, seed=SEED, op=op)
+    E, N = mesh.nbElem, mesh.nbNodes
+    a = minifem.Assembler(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("reference")
+    a.set_coefficients(op, mesh.coef)
+    markf = O.checkbounds(mesh.boundNodesCode)
+    a.set_check_bounds(markf)
+    ncol = a.coloring_creation(seed=1)[1].size - 1
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    timed = _timer(torch, torch.cuda.ExternalStream(a.stream), flush)
+    res = {}
+    for name, prec, strat in (("fp64_gather", "fp64", "gather"), ("fp64_scatter", "fp64", "scatter"),
+                              ("fp64_atomic", "fp64", "atomic"), ("fp32_tiles", "fp32", "gather")):
+        ms = timed(lambda: a.assembly(op, prec, strat, prec=True), args.steps, args.warmup)
+        res[name] = {"ms_per_step": round(ms, 4), "value": round(E / (ms * 1e-3) / 1e6, 1)}
+    a.assembly(op, "fp64", "gather", prec=True)
+    ref = O.full(mesh, op=op)
+    bit_exact = (a.values().tobytes() == ref["values"].tobytes()
+                 and a.prec().tobytes() == ref["prec"].tobytes())
+    t = []
+    for _ in range(max(3, args.cpu_iters)):
+        t0 = time.perf_counter()
+        v = O.assembly(mesh.coord, ref["row"], ref["col"], mesh.elemToNode, int(ref["row"][-1]), op,
+                       mesh.coef)
+        O.prec(v, ref["row"], ref["col"], markf, N, op)
+        t.append(time.perf_counter() - t0)
+    cpu = E / statistics.mean(t) / 1e6
+    return {"metric": f"{op} assembly + preconditioner Melem/s @146k tets (FP64 gather)",
+            "value": res["fp64_gather"]["value"], "unit": "Melem/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": res["fp64_gather"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{op}_cube30_146k_tets", "nbElem": E, "nbNodes": N,
+                       "nbEdges": len(col), "colours": ncol},
+            "variants": res, "bit_exact_vs_oracle": bit_exact,
+            "cpu_baseline": {"value": round(cpu, 3), "unit": "Melem/s", "cores": 1, "kind": "port",
+                             "sample": f"{len(t)} iterations of the same mesh"}}
+
+
+def run_stress(args):
+    """60^3 stress cube (1,232,274 tets): jitter 0.45h, 5% slivers, E jump 1e6,
+    nu up to 0.45; FP32 with FP64 slivers and block inverse against all-FP64."""
+    import torch
+    import minifem
+    import pyoracle as O
+    from minifem import metrics
+    from minifem.meshgen import cube_mesh
+    mesh = cube_mesh(60, seed=SEED, op="ela", jitter=0.45, sliver_fraction=0.05, jump=1e6,
+                     nu_max=0.45)
+    E, N = mesh.nbElem, mesh.nbNodes
+    a = minifem.Assembler(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    a.set_coefficients("ela", mesh.coef)
+    a.set_check_bounds(O.checkbounds(mesh.boundNodesCode))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    timed = _timer(torch, torch.cuda.ExternalStream(a.stream), flush)
+    t32 = timed(lambda: a.assembly("ela", "fp32", "gather", prec=True), args.steps, args.warmup)
+    flagged = a.flagged()
+    v32, p32 = a.values(), a.prec()
+    t64 = timed(lambda: a.assembly("ela", "fp64", "gather", prec=True), args.steps, args.warmup)
+    v64, p64 = a.values(), a.prec()
+    err = metrics.entry_errors(row, col, v64, v32, 9)
+    err["preconditioned_operator_rel"] = metrics.operator_error(row, col, v64, p64, v32, p32, 9)
+    return {"metric": "ela stress mesh Melem/s @1.23M tets (FP32, FP64 slivers + block inverse)",
+            "value": round(E / (t32 * 1e-3) / 1e6, 1), "unit": "Melem/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t32, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: jitter 0.45h, slivers (aspect up to 1e4), E jump 1e6, nu <= 0.45",
+            "config": {"workload": "ela_stress60_1.23M_tets", "nbElem": E, "nbNodes": N,
+                       "nbEdges": len(col), "slivers_made": mesh.meta.get("slivers_made")},
+            "flagged_fp64_elements": flagged,
+            "fp64_plain": {"value": round(E / (t64 * 1e-3) / 1e6, 1), "ms_per_step": round(t64, 4)},
+            "fp32_errors_vs_fp64": err}
+
+
+def run_batch(args):
+    """64 meshes, n ~ U{12..60} nodes per side (seeded), half lap half ela, 8
+    coefficient sets each, re-assembled per iteration by one graph replay."""
+    import torch
+    import minifem
+    import pyoracle as O
+    from minifem.meshgen import cube_mesh, rng_u64
+    sides = 12 + (rng_u64(SEED, 99, 64) % np.uint64(49)).astype(int)
+    batch = minifem.Batch(0)
+    asms = []
+    total_e = total_asm = 0
+    for i, n in enumerate(sides):
+        op = "lap" if i % 2 == 0 else "ela"
+        meshes = [cube_mesh(int(n), seed=SEED + 1000 * i + s, op=op) for s in range(8)]
+        m = meshes[0]
+        a = minifem.Assembler(0)
+        a.set_mesh(m.coord, m.elemToNode)
+        a.create_nodeToNode("sorted")
+        a.set_check_bounds(O.checkbounds(m.boundNodesCode))
+        batch.add(a, op, np.stack([mm.coef for mm in meshes]))
+        asms.append(a)
+        total_e += m.nbElem
+        total_asm += 8 * m.nbElem
+    info = batch.info()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    timed = _timer(torch, torch.cuda.ExternalStream(batch.stream), flush)
+    t32 = timed(lambda: batch.assemble("fp32", prec=True), args.steps, args.warmup)
+    t64 = timed(lambda: batch.assemble("fp64", prec=True), max(1, args.steps // 2), 1)
+    batch.synchronize()
+    return {"metric": "batched assembly + preconditioner, element-assemblies/s (64 meshes x 8 sets)",
+            "value": round(total_asm / (t32 * 1e-3) / 1e6, 1), "unit": "Melem/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t32, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: 64 jittered permuted cubes, n ~ U{12..60}, half lap half ela, "
+                    "8 coefficient sets each",
+            "config": {"workload": "batch64x8", "meshes": len(sides), "sets": 8,
+                       "elements": total_e, "element_assemblies": total_asm,
+                       "tiles": info["work"], "persistent_grid": info["grid"],
+                       "launch": "one CUDA graph per iteration; FP32 = one persistent kernel"},
+            "fp64_plain": {"value": round(total_asm / (t64 * 1e-3) / 1e6, 1),
+                           "ms_per_step": round(t64, 4)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,6 +549,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--workload", default="ela100",
+                    choices=["ela100", "ela30", "lap30", "stress60", "batch64"],
+                    help="ela100: the benchmark line; the others: the remaining configurations")
     ap.add_argument("--side", type=int, default=N_SIDE,
                     help="nodes per cube side (100 = the benchmark mesh; smaller for profiling)")
     args = ap.parse_args()
@@ -380,8 +571,16 @@ def main():
     try:
         if args.impl == "reference":
             out = run_reference(args, rank, world)
-        else:
+        elif args.workload == "ela100":
             out = run_ours(args, rank, world, local_rank)
+        elif rank != 0:
+            out = None
+        elif args.workload in ("ela30", "lap30"):
+            out = run_cube30(args, args.workload[:3])
+        elif args.workload == "stress60":
+            out = run_stress(args)
+        else:
+            out = run_batch(args)
         if out is not None:
             print(json.dumps(out), flush=True)
     finally:
