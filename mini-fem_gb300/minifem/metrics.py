@@ -60,9 +60,10 @@ def operator_error(row, col, ref_vals, ref_prec, vals, prec, dim: int, seed: int
                    nvec: int = 3) -> float:
     rng = np.random.default_rng(seed)
     N = len(row) - 1
+    bs = 1 if dim == 1 else 3
     worst = 0.0
     for _ in range(nvec):
-        x = rng.standard_normal(N * dim)
+        x = rng.standard_normal(N * bs)
         y0 = _apply(row, col, np.asarray(ref_vals, np.float64), ref_prec, dim, x)
         y1 = _apply(row, col, np.asarray(vals, np.float64), prec, dim, x)
         worst = max(worst, float(np.linalg.norm(y1 - y0) / np.linalg.norm(y0)))
