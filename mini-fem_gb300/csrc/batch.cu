@@ -160,8 +160,7 @@ void prepare(mfem_batch &b) {
         auto *it = b.items[m];
         Context &c = it->ctx->c;
         BatchMesh &B = tab[m];
-        B.geo.hi = hi + it->nodeOff;
-        B.geo.lo = hi + b.totalNodes + it->nodeOff;
+        B.geo.hl = hi + 2 * it->nodeOff;
         B.geo.coord = c.coord.as<double>();
         B.geo.e2n = c.e2n.as<int4>();
         B.geo.diagPos = c.diagPos.as<int>();
@@ -204,7 +203,7 @@ void record32(mfem_batch &b, bool withPrec) {
     float4 *hi = b.hilo.as<float4>();
     for (auto *it : b.items) {
         Context &c = it->ctx->c;
-        split_coords(c, hi + it->nodeOff, hi + b.totalNodes + it->nodeOff, b.stream);
+        split_coords(c, hi + 2 * it->nodeOff, b.stream);
         const long long n = (long long)c.nbElem * (it->hasCoef ? it->nSets : 1);
         weights32_all(it->op, it->hasCoef ? it->coef.as<double>() : nullptr, n, it->w32.as<float2>(),
                       b.stream);

@@ -37,7 +37,7 @@ struct TilePlan {
     long long nUnits = 0;       // off-diagonal units (an intra-tile pair counts once)
     long long nContrib = 0;     // contributions summed per coefficient set
     SmemLayout layout{};
-    DevBuf desc, elems, conn, offEnt, diagEnt, contrib;
+    DevBuf desc, elems, lconn, nodes, offEnt, diagEnt, contrib;
     DevBuf w32;                 // per-element weights of the current coefficients
 };
 
@@ -130,7 +130,7 @@ void build_gather_plan(Context &c);
 void build_tile_plan(Context &c);
 void assemble_tiles32(Context &c, int op, bool fusePrec);
 TilePlanView plan_view(const TilePlan &tp);
-void split_coords(const Context &c, float4 *hi, float4 *lo, cudaStream_t s);
+void split_coords(const Context &c, float4 *hl, cudaStream_t s);
 void weights32_all(int op, const double *coef, long long n, float2 *w, cudaStream_t s);
 
 // coloring.cu

@@ -33,10 +33,9 @@ __device__ __forceinline__ ElemCoords load_coords(const float4 *__restrict__ hi,
 }
 
 // Gradients g[4][3] of one element in FP32 from its loaded coordinates.
-// Returns true when the element was flagged (quality |6V| / (|a||b||c|) below
-// sqrt(qthr2)) and computed in FP64 from `coord` instead.
-__device__ __forceinline__ bool grad32_from(const ElemCoords &C, const double *__restrict__ coord,
-                                            int4 nd, float qthr2, float g[12]) {
+// Returns true, with g not computed, when the element is flagged: quality
+// |6V| / (|a||b||c|) below sqrt(qthr2).
+__device__ __forceinline__ bool grad32_core(const ElemCoords &C, float qthr2, float g[12]) {
     const float xa = (C.h0.x - C.h3.x) + (C.l0.x - C.l3.x), ya = (C.h0.y - C.h3.y) + (C.l0.y - C.l3.y),
                 za = (C.h0.z - C.h3.z) + (C.l0.z - C.l3.z);
     const float xb = (C.h2.x - C.h3.x) + (C.l2.x - C.l3.x), yb = (C.h2.y - C.h3.y) + (C.l2.y - C.l3.y),
@@ -50,13 +49,7 @@ __device__ __forceinline__ bool grad32_from(const ElemCoords &C, const double *_
     const float na = fmaf(xa, xa, fmaf(ya, ya, za * za));
     const float nb = fmaf(xb, xb, fmaf(yb, yb, zb * zb));
     const float nc = fmaf(xc, xc, fmaf(yc, yc, zc * zc));
-    if (vol * vol < qthr2 * (na * nb) * nc) {
-        double gd[12];
-        elem_gradients(coord, nd, gd);
-#pragma unroll
-        for (int i = 0; i < 12; i++) g[i] = __double2float_rn(gd[i]);
-        return true;
-    }
+    if (vol * vol < qthr2 * (na * nb) * nc) return true;
     g[9] = -((g[0] + g[3]) + g[6]);
     g[10] = -((g[1] + g[4]) + g[7]);
     g[11] = -((g[2] + g[5]) + g[8]);
@@ -64,6 +57,23 @@ __device__ __forceinline__ bool grad32_from(const ElemCoords &C, const double *_
 #pragma unroll
     for (int i = 0; i < 12; i++) g[i] *= r;
     return false;
+}
+
+// Gradients of a flagged element: the FP64 formula, rounded to FP32.
+__device__ __forceinline__ void grad32_fp64(const double *__restrict__ coord, int4 nd, float g[12]) {
+    double gd[12];
+    elem_gradients(coord, nd, gd);
+#pragma unroll
+    for (int i = 0; i < 12; i++) g[i] = __double2float_rn(gd[i]);
+}
+
+// grad32_core, with flagged elements computed in FP64 from `coord`; returns
+// whether the element was flagged.
+__device__ __forceinline__ bool grad32_from(const ElemCoords &C, const double *__restrict__ coord,
+                                            int4 nd, float qthr2, float g[12]) {
+    if (!grad32_core(C, qthr2, g)) return false;
+    grad32_fp64(coord, nd, g);
+    return true;
 }
 
 __device__ __forceinline__ bool grad32(const float4 *__restrict__ hi, const float4 *__restrict__ lo,

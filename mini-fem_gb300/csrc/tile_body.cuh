@@ -11,11 +11,6 @@
 namespace mfem {
 namespace tilek {
 
-// Phase 1 can load two elements per thread before computing either (more loads
-// in flight per thread, more registers); measured slower on the 100^3 cube
-// (0.99 vs 0.90 ms), so one element per pass.
-constexpr bool kPairLoads = false;
-
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
@@ -147,71 +142,88 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     int4 *sOff = reinterpret_cast<int4 *>(sm + L.off);
     int2 *sDiag = reinterpret_cast<int2 *>(sm + L.diag);
     float *sRes = reinterpret_cast<float *>(sm + L.res);              // 12 floats per row
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);           // two barriers
     const int tid = threadIdx.x;
 
-    // 0. stage the plan segments with the TMA engine
+    // 0. stage the entry tables with the TMA engine (barrier 0)
     if (tid == 0) {
         mbar_init(bar, 1);
-        // make the initialised barrier visible to the TMA (async) proxy
+        mbar_init(bar + 1, 1);
+        // make the initialised barriers visible to the TMA (async) proxy
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const unsigned bc = (unsigned)T.nContribPad * 2u, bo = (unsigned)T.nOffPad * 16u,
-                       bd = (unsigned)T.nRowsPad * 8u;
-        mbar_expect_tx(bar, bc + bo + bd + ctl.extraTx);
-        if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar);
+        const unsigned bo = (unsigned)T.nOffPad * 16u, bd = (unsigned)T.nRowsPad * 8u;
+        mbar_expect_tx(bar, bo + bd + ctl.extraTx);
         if (bo) bulk_g2s(sOff, P.offEnt + T.offBegin, bo, bar);
         if (bd) bulk_g2s(sDiag, P.diagEnt + T.diagBegin, bd, bar);
     }
 
-    // 1. gradients of the tile's elements (and the weights of set 0); with
-    //    kPairLoads two elements per thread per pass, all their loads issued first
+    // 1a. the tile's node coordinates (hi and lo parts) into the contribution
+    //     region, which the contribution lists fill only after phase 1
+    float4 *Xh = reinterpret_cast<float4 *>(sm + L.contrib);
+    float4 *Xl = Xh + T.nNodes;
+    for (int i = tid; i < T.nNodes; i += kTileThreads) {
+        const int n = P.nodes[T.nodeBegin + i];
+        Xh[i] = M.hl[2 * n];
+        Xl[i] = M.hl[2 * n + 1];
+    }
+    // the first element's connectivity and weights load meanwhile
+    ushort4 lc = make_ushort4(0, 0, 0, 0);
+    float2 w = make_float2(0.f, 0.f);
+    if (tid < T.nElem) {
+        lc = P.lconn[T.elemBegin + tid];
+        w = S.w[P.elems[T.elemBegin + tid]];
+    }
+    __syncthreads();
+
+    // 1b. gradients of the tile's elements and the weights of set 0
     int flagged = 0;
-    if constexpr (kPairLoads) {
-        for (int i0 = tid; i0 < T.nElem; i0 += 2 * kTileThreads) {
-            const int i1 = i0 + kTileThreads;
-            const bool has1 = i1 < T.nElem;
-            const int4 n0 = P.conn[T.elemBegin + i0];
-            const int4 n1 = has1 ? P.conn[T.elemBegin + i1] : n0;
-            const int e0 = P.elems[T.elemBegin + i0];
-            const int e1 = has1 ? P.elems[T.elemBegin + i1] : e0;
-            const ElemCoords c0 = load_coords(M.hi, M.lo, n0);
-            const ElemCoords c1 = load_coords(M.hi, M.lo, n1);
-            const float2 w0 = S.w[e0], w1 = S.w[e1];
-            float g[12];
-            flagged += grad32_from(c0, M.coord, n0, qthr2, g);
-#pragma unroll
-            for (int j = 0; j < 4; j++) G[4 * i0 + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
-            W[i0] = w0;
-            if (has1) {
-                flagged += grad32_from(c1, M.coord, n1, qthr2, g);
-#pragma unroll
-                for (int j = 0; j < 4; j++) G[4 * i1 + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
-                W[i1] = w1;
-            }
+    for (int i = tid; i < T.nElem; i += kTileThreads) {
+        const int inext = i + kTileThreads;
+        ushort4 lcn = lc;
+        float2 wn = w;
+        if (inext < T.nElem) {
+            lcn = P.lconn[T.elemBegin + inext];
+            wn = S.w[P.elems[T.elemBegin + inext]];
         }
-    } else {
-        for (int i = tid; i < T.nElem; i += kTileThreads) {
-            const int4 nd = P.conn[T.elemBegin + i];
-            const float2 w = S.w[P.elems[T.elemBegin + i]];
-            float g[12];
-            flagged += grad32(M.hi, M.lo, M.coord, nd, qthr2, g);
-#pragma unroll
-            for (int j = 0; j < 4; j++) G[4 * i + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
-            W[i] = w;
+        ElemCoords C;
+        C.h0 = Xh[lc.x]; C.h1 = Xh[lc.y]; C.h2 = Xh[lc.z]; C.h3 = Xh[lc.w];
+        C.l0 = Xl[lc.x]; C.l1 = Xl[lc.y]; C.l2 = Xl[lc.z]; C.l3 = Xl[lc.w];
+        float g[12];
+        if (grad32_core(C, qthr2, g)) {
+            const int *nb = P.nodes + T.nodeBegin;
+            grad32_fp64(M.coord, make_int4(nb[lc.x], nb[lc.y], nb[lc.z], nb[lc.w]), g);
+            flagged++;
         }
+#pragma unroll
+        for (int j = 0; j < 4; j++) G[4 * i + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
+        W[i] = w;
+        lc = lcn;
+        w = wn;
     }
     if (flagged) atomicAdd(counters + 1, flagged);
     __syncthreads();
 
+    // the contribution lists (barrier 1), over the node coordinates: the
+    // generic-proxy reads above are ordered before the async-proxy writes
+    if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const unsigned bc = (unsigned)T.nContribPad * 2u;
+        mbar_expect_tx(bar + 1, bc);
+        if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar + 1);
+    }
     // bounded wait for the staged segments (the CTA agrees on the outcome)
     bool ok = false;
-    for (unsigned it = 0; it < ctl.waitLimit && !ok; it++) ok = mbar_try_wait(bar, 0);
+    for (unsigned it = 0; it < ctl.waitLimit && !ok; it++)
+        ok = mbar_try_wait(bar, 0) && mbar_try_wait(bar + 1, 0);
     if (__syncthreads_or(!ok)) {
         if (tid == 0) atomicOr(counters + 2, 1);
         return false;
     }
-    if (tid == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+    if (tid == 0) {
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar + 1)) : "memory");
+    }
 
     for (int set = 0; set < S.nSets; set++) {
         float *values = S.values + (size_t)set * S.valuesStride;

@@ -4,11 +4,14 @@
 // tiles of at most maxRows rows whose incident elements number at most maxElem.
 // One CTA per tile:
 //   0. one thread starts TMA bulk copies (cp.async.bulk, completion on an
-//      mbarrier) of the tile's contiguous plan segments -- contribution lists,
-//      off-diagonal entry table, diagonal table -- into shared memory;
-//   1. meanwhile every thread computes FP32 gradients and weights of the
-//      elements incident to the tile's rows (ascending element id) into shared
-//      memory: each element once per tile that needs it, no records in HBM;
+//      mbarrier) of the tile's off-diagonal entry table and diagonal table;
+//   1. meanwhile the CTA gathers the coordinates of the tile's nodes (one
+//      32-byte sector per node) into shared memory, then computes the FP32
+//      gradients and weights of the elements incident to the tile's rows
+//      (ascending element id, connectivity as indices into the tile's node
+//      list) into shared memory: each element once per tile that needs it, no
+//      records in HBM; the contribution lists are then copied (second
+//      mbarrier) over the node coordinates, which are no longer needed;
 //   2. one thread per off-diagonal entry sums its contributions with Kahan
 //      compensation and writes the 3x3 block (or scalar) to the CSR values;
 //   3. four lanes per diagonal entry sum a quarter of its contributions each,
@@ -49,15 +52,16 @@ __global__ void k_weights32(const double *__restrict__ coef, long long n, float2
     if (i < n) w[i] = weights32<OP>(coef, (int)i);
 }
 
+// hi and lo parts of node i side by side (hl[2i], hl[2i+1]): one 32-byte sector
 __global__ void k_split_coords_t(const double *__restrict__ coord, int nbNodes,
-                                 float4 *__restrict__ hi, float4 *__restrict__ lo) {
+                                 float4 *__restrict__ hl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbNodes) return;
     const double x = coord[3 * i], y = coord[3 * i + 1], z = coord[3 * i + 2];
     const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
-    hi[i] = make_float4(xh, yh, zh, 0.f);
-    lo[i] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
-                        __double2float_rn(z - (double)zh), 0.f);
+    hl[2 * i] = make_float4(xh, yh, zh, 0.f);
+    hl[2 * i + 1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
+                                __double2float_rn(z - (double)zh), 0.f);
 }
 
 uint32_t spread3(uint32_t v) {   // 10 bits -> every third bit
@@ -73,15 +77,15 @@ int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
 }  // namespace
 
-SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad) {
+SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes) {
     SmemLayout L;
     L.w = maxElem * 64;                                 // gradients: 4 float4 per element
     L.contrib = L.w + round_up(maxElem * 8, 16);        // weights: float2 per element
-    L.off = L.contrib + round_up(maxContribPad * 2, 16);
+    L.off = L.contrib + round_up(std::max(maxContribPad * 2, maxNodes * 32), 16);
     L.diag = L.off + maxOffPad * 16;
     L.res = L.diag + maxRowsPad * 8;
     L.bar = L.res + round_up(maxRowsPad * 48, 16);      // 12 floats per row
-    L.bytes = L.bar + 16;
+    L.bytes = L.bar + 16;                               // two mbarriers
     return L;
 }
 
@@ -133,7 +137,11 @@ void build_tile_plan(Context &c) {
     contrib.reserve((size_t)E * 16 + (size_t)N);
     std::vector<int> mark(E, -1), local(E, 0), elems, rows, cnt, fill, start, keep;
     std::vector<int> rowTile(N, -1), rowLocal(N, 0);
-    int maxElem = 0, maxContrib = 0, maxOff = 0, maxRows = 0;
+    std::vector<int> tileNodes, nodeMark(N, -1), nodeLocal(N, 0), tn;
+    std::vector<ushort4> lconn;
+    tileNodes.reserve((size_t)N * 4);
+    lconn.reserve((size_t)E * 3);
+    int maxElem = 0, maxContrib = 0, maxOff = 0, maxRows = 0, maxNodes = 0;
 
     int i = 0;
     while (i < N) {
@@ -164,6 +172,26 @@ void build_tile_plan(Context &c) {
         T.elemBegin = (int)tileElems.size();
         T.nElem = (int)elems.size();
         tileElems.insert(tileElems.end(), elems.begin(), elems.end());
+        // the nodes of the tile's elements, and the elements' nodes as indices into them
+        tn.clear();
+        for (int e : elems)
+            for (int k = 0; k < 4; k++) {
+                const int n = e2n[4 * (size_t)e + k];
+                if (nodeMark[n] != tIndex) {
+                    nodeMark[n] = tIndex;
+                    tn.push_back(n);
+                }
+            }
+        std::sort(tn.begin(), tn.end());
+        for (int k = 0; k < (int)tn.size(); k++) nodeLocal[tn[k]] = k;
+        T.nodeBegin = (int)tileNodes.size();
+        T.nNodes = (int)tn.size();
+        tileNodes.insert(tileNodes.end(), tn.begin(), tn.end());
+        for (int e : elems) {
+            const size_t b4 = 4 * (size_t)e;
+            lconn.push_back(make_ushort4((unsigned short)nodeLocal[e2n[b4]], (unsigned short)nodeLocal[e2n[b4 + 1]],
+                                         (unsigned short)nodeLocal[e2n[b4 + 2]], (unsigned short)nodeLocal[e2n[b4 + 3]]));
+        }
         T.offBegin = (int)offEnt.size();
         T.diagBegin = (int)diagEnt.size();
         T.contribBegin = (int)contrib.size();
@@ -246,12 +274,13 @@ void build_tile_plan(Context &c) {
         maxContrib = std::max(maxContrib, T.nContribPad);
         maxOff = std::max(maxOff, T.nOffPad);
         maxRows = std::max(maxRows, T.nRowsPad);
+        maxNodes = std::max(maxNodes, T.nNodes);
         tiles.push_back(T);
     }
     MFEM_REQUIRE(tp.maxElem <= 4096, MFEM_ERR_CAPACITY, "tile plan: local index overflow");
 
     tp.nTiles = (int)tiles.size();
-    tp.layout = smem_layout(std::max(maxElem, 1), maxContrib, maxOff, maxRows);
+    tp.layout = smem_layout(std::max(maxElem, 1), maxContrib, maxOff, maxRows, maxNodes);
     MFEM_REQUIRE(tp.layout.bytes <= 227 * 1024, MFEM_ERR_CAPACITY,
                  "tile plan: a tile needs more than 227 KB of shared memory");
     auto up = [&](DevBuf &d, const void *src, size_t bytes) {
@@ -260,14 +289,8 @@ void build_tile_plan(Context &c) {
     };
     up(tp.desc, tiles.data(), tiles.size() * sizeof(TileDesc));
     up(tp.elems, tileElems.data(), tileElems.size() * 4);
-    {
-        std::vector<int4> conn(tileElems.size());
-        for (size_t k = 0; k < tileElems.size(); k++) {
-            const size_t e = (size_t)tileElems[k];
-            conn[k] = make_int4(e2n[4 * e], e2n[4 * e + 1], e2n[4 * e + 2], e2n[4 * e + 3]);
-        }
-        up(tp.conn, conn.data(), conn.size() * sizeof(int4));
-    }
+    up(tp.lconn, lconn.data(), lconn.size() * sizeof(ushort4));
+    up(tp.nodes, tileNodes.data(), tileNodes.size() * 4);
     up(tp.offEnt, offEnt.data(), offEnt.size() * sizeof(int4));
     up(tp.diagEnt, diagEnt.data(), diagEnt.size() * sizeof(int2));
     up(tp.contrib, contrib.data(), contrib.size() * 2);
@@ -286,7 +309,8 @@ TilePlanView plan_view(const TilePlan &tp) {
     TilePlanView P;
     P.desc = tp.desc.as<TileDesc>();
     P.elems = tp.elems.as<int>();
-    P.conn = tp.conn.as<int4>();
+    P.lconn = tp.lconn.as<ushort4>();
+    P.nodes = tp.nodes.as<int>();
     P.offEnt = tp.offEnt.as<int4>();
     P.diagEnt = tp.diagEnt.as<int2>();
     P.contrib = tp.contrib.as<unsigned short>();
@@ -299,8 +323,8 @@ void weights32_all(int op, const double *coef, long long n, float2 *w, cudaStrea
     check_launch("k_weights32");
 }
 
-void split_coords(const Context &c, float4 *hi, float4 *lo, cudaStream_t s) {
-    k_split_coords_t<<<blocks_for(c.nbNodes, 256), 256, 0, s>>>(c.coord.as<double>(), c.nbNodes, hi, lo);
+void split_coords(const Context &c, float4 *hl, cudaStream_t s) {
+    k_split_coords_t<<<blocks_for(c.nbNodes, 256), 256, 0, s>>>(c.coord.as<double>(), c.nbNodes, hl);
     check_launch("k_split_coords_t");
 }
 
@@ -311,18 +335,16 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     const int dim = op == MFEM_OP_LAP ? 1 : 9;
     c.values.reserve(sizeof(float) * (size_t)c.nnz * dim);
     double *prec = fusePrec ? (double *)c.prec.reserve(sizeof(double) * (size_t)N * dim) : nullptr;
-    float4 *hi = (float4 *)c.scratch.reserve(sizeof(float4) * 2 * (size_t)N);
-    float4 *lo = hi + N;
+    float4 *hl = (float4 *)c.scratch.reserve(sizeof(float4) * 2 * (size_t)N);
     float2 *w = (float2 *)c.tiles.w32.reserve(sizeof(float2) * (size_t)c.nbElem);
     c.timer.begin("split_coords+weights", c.stream);
-    split_coords(c, hi, lo, c.stream);
+    split_coords(c, hl, c.stream);
     weights32_all(op, c.coefOp == op ? c.coef.as<double>() : nullptr, c.nbElem, w, c.stream);
     c.timer.end(c.stream);
     int *st = status_ptr(c);
     MFEM_CUDA(cudaMemsetAsync(st + 4, 0, sizeof(int) * 3, c.stream));
     TileMesh M;
-    M.hi = hi;
-    M.lo = lo;
+    M.hl = hl;
     M.coord = c.coord.as<double>();
     M.e2n = c.e2n.as<int4>();
     M.diagPos = c.diagPos.as<int>();

@@ -15,6 +15,7 @@ struct TileDesc {
     int elemBegin, nElem;                    // into elems
     int offBegin, nOff, nOffPad;             // into offEnt: (pos, transposed pos or -1, meta, 0)
     int contribBegin, nContrib, nContribPad; // into contrib (u16: local elem << 4 | j << 2 | k)
+    int nodeBegin, nNodes;                   // into nodes: the nodes of the tile's elements
     int mesh;                                // batch: index of the mesh the tile belongs to
 };
 
@@ -23,7 +24,8 @@ struct TileDesc {
 struct TilePlanView {
     const TileDesc *desc;
     const int *elems;            // element ids of each tile (ascending)
-    const int4 *conn;            // their 0-based nodes, in the same order
+    const ushort4 *lconn;        // their nodes as indices into the tile's node list
+    const int *nodes;            // each tile's nodes (0-based ids, ascending)
     const int4 *offEnt;
     const int2 *diagEnt;
     const unsigned short *contrib;
@@ -31,7 +33,7 @@ struct TilePlanView {
 
 // Per-mesh geometry the tile kernel reads.
 struct TileMesh {
-    const float4 *hi, *lo;       // coordinates split into float hi + lo
+    const float4 *hl;            // coordinates split into float hi + lo: hl[2n], hl[2n+1]
     const double *coord;         // FP64 coordinates (slivers)
     const int4 *e2n;             // 0-based connectivity
     const int *diagPos;
@@ -60,11 +62,13 @@ struct TileCtl {
     unsigned extraTx;
 };
 
-// Byte offsets of the dynamic shared-memory regions.
+// Byte offsets of the dynamic shared-memory regions.  The contribution region
+// holds the tile's node coordinates (32 bytes per node) while the gradients are
+// computed, then the contribution lists.
 struct SmemLayout {
     int w, contrib, off, diag, res, bar, bytes;
 };
 
-SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad);
+SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes);
 
 }  // namespace mfem

@@ -21,7 +21,7 @@ import json
 import os
 import statistics
 
-TILE_CANDIDATES = [(32, 320), (64, 640), (96, 960), (128, 1280)]
+TILE_CANDIDATES = [(40, 448), (48, 512), (48, 544), (56, 576), (64, 640), (96, 960)]
 
 
 def _device_name(device: int) -> str:
