@@ -109,20 +109,33 @@ __device__ __forceinline__ void ela_diag_accumulate(Kahan *acc, float4 g, float 
     acc[5].add(g.y * bz);
 }
 
-// Inverse of a symmetric 3x3 block by its six distinct cofactors (FP64, FMAs);
-// d = (d00, d11, d22, d01, d02, d12).  Returns false for an exactly singular
-// block, which is then left as it is.
-__device__ __forceinline__ bool inv3_sym(double d[6]) {
-    const double a = d[0], e = d[1], i = d[2], b = d[3], c = d[4], f = d[5];
-    const double c00 = fma(e, i, -f * f);
-    const double c01 = fma(c, f, -b * i);
-    const double c02 = fma(b, f, -c * e);
-    const double det = fma(a, c00, fma(b, c01, c * c02));
-    if (det == 0.0) return false;
-    const double r = 1.0 / det;
-    const double c11 = fma(a, i, -c * c);
-    const double c12 = fma(b, c, -a * f);
-    const double c22 = fma(a, e, -b * b);
+// Inverse of a symmetric 3x3 block by its six distinct cofactors in FP32;
+// d = (d00, d11, d22, d01, d02, d12).  The block is first scaled by the power
+// of two 2^-k that brings its largest diagonal entry to [1, 2) (exact), so that
+// the cofactors (products of two entries) and the determinant (of three) stay
+// inside the FP32 range for any entry magnitude; the inverse of the scaled
+// block times 2^-k is the inverse.  Every cofactor is a 2x2 determinant
+// a*b - c*d evaluated with Kahan's FMA method (within about one ulp), the
+// determinant is their FMA dot product with the first row, and the inverse
+// entries are cofactor * (1 / det): a few ulps relative error per entry for
+// the block given.  Returns false for an exactly singular block, which is then
+// left as it is.
+__device__ __forceinline__ bool inv3_sym32(float d[6]) {
+    const float mx = fmaxf(fabsf(d[0]), fmaxf(fabsf(d[1]), fabsf(d[2])));
+    if (!(mx > 0.f) || mx > 3.0e38f) return false;   // zero, NaN or infinite diagonal
+    const int ex = min(max((int)((__float_as_uint(mx) >> 23) & 0xffu) - 127, -126), 126);
+    const float sc = __uint_as_float((unsigned)(127 - ex) << 23);   // 2^-ex, a normal float
+    const float a = d[0] * sc, e = d[1] * sc, i = d[2] * sc, b = d[3] * sc, c = d[4] * sc,
+                f = d[5] * sc;
+    const float c00 = diff_prod(e, i, f, f);
+    const float c01 = diff_prod(c, f, b, i);
+    const float c02 = diff_prod(b, f, c, e);
+    const float det = fmaf(a, c00, fmaf(b, c01, c * c02));
+    if (det == 0.f) return false;
+    const float r = sc / det;
+    const float c11 = diff_prod(a, i, c, c);
+    const float c12 = diff_prod(b, c, a, f);
+    const float c22 = diff_prod(a, e, b, b);
     d[0] = c00 * r; d[1] = c11 * r; d[2] = c22 * r;
     d[3] = c01 * r; d[4] = c02 * r; d[5] = c12 * r;
     return true;
@@ -319,22 +332,20 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         }
         __syncthreads();
         // 3b. one thread per row: write the diagonal block and the preconditioner
-        //     (full warps on the FP64 pipe)
+        //     (inverted in FP32, stored as FP64)
         for (int rl = tid; rl < T.nRows; rl += kTileThreads) {
             const int r = sDiag[rl].x;
             const int p = M.diagPos[r];
             if (OP == MFEM_OP_LAP) {
                 const float s = sRes[12 * rl], c = sRes[12 * rl + 1];
                 if (p >= 0) values[p] = s - c;
-                if (PREC) precOut[r] = 1.0 / (f32_to_f64(s) - f32_to_f64(c));
+                if (PREC) precOut[r] = f32_to_f64(1.0f / (s - c));
             } else {
-                float sv[6];
-                double d[6];
+                float sv[6], d[6];
 #pragma unroll
                 for (int m = 0; m < 6; m++) {
-                    const float s = sRes[12 * rl + 2 * m], c = sRes[12 * rl + 2 * m + 1];
-                    sv[m] = s - c;
-                    if (PREC) d[m] = f32_to_f64(s) - f32_to_f64(c);
+                    sv[m] = sRes[12 * rl + 2 * m] - sRes[12 * rl + 2 * m + 1];
+                    d[m] = sv[m];
                 }
                 if (p >= 0) {
                     float *v = values + (size_t)p * 9;
@@ -347,15 +358,18 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                         // src/Fortran/elasclpr.f:19-27: constrained DOF k -> row and
                         // column k of the block zero, diagonal 1
                         const unsigned mk = M.mask[r];
-                        if (mk & 1u) { d[0] = 1.0; d[3] = 0.0; d[4] = 0.0; }
-                        if (mk & 2u) { d[1] = 1.0; d[3] = 0.0; d[5] = 0.0; }
-                        if (mk & 4u) { d[2] = 1.0; d[4] = 0.0; d[5] = 0.0; }
+                        if (mk & 1u) { d[0] = 1.f; d[3] = 0.f; d[4] = 0.f; }
+                        if (mk & 2u) { d[1] = 1.f; d[3] = 0.f; d[5] = 0.f; }
+                        if (mk & 4u) { d[2] = 1.f; d[4] = 0.f; d[5] = 0.f; }
                     }
-                    if (p >= 0 && !inv3_sym(d)) atomicAdd(counters, 1);
+                    if (p >= 0 && !inv3_sym32(d)) atomicAdd(counters, 1);
+                    double x[6];
+#pragma unroll
+                    for (int m = 0; m < 6; m++) x[m] = f32_to_f64(d[m]);
                     double *o = precOut + (size_t)r * 9;   // 72-byte blocks: 8-byte aligned
-                    o[0] = d[0]; o[1] = d[3]; o[2] = d[4];
-                    o[3] = d[3]; o[4] = d[1]; o[5] = d[5];
-                    o[6] = d[4]; o[7] = d[5]; o[8] = d[2];
+                    o[0] = x[0]; o[1] = x[3]; o[2] = x[4];
+                    o[3] = x[3]; o[4] = x[1]; o[5] = x[5];
+                    o[6] = x[4]; o[7] = x[5]; o[8] = x[2];
                 }
             }
         }
