@@ -97,6 +97,45 @@ __device__ __forceinline__ void ela_accumulate(Kahan *acc, float4 gj, float4 gk,
     }
 }
 
+// One 3x3 FP32 block to base[9p .. 9p+8] with four 8-byte stores and one
+// 4-byte store (which one comes first depends on the address), instead of nine
+// 4-byte stores: fewer memory transactions per block.
+__device__ __forceinline__ void store_block9(float *base, size_t p, const float v[9]) {
+    float *o = base + p * 9;
+    if (reinterpret_cast<uintptr_t>(o) & 7u) {
+        o[0] = v[0];
+        *reinterpret_cast<float2 *>(o + 1) = make_float2(v[1], v[2]);
+        *reinterpret_cast<float2 *>(o + 3) = make_float2(v[3], v[4]);
+        *reinterpret_cast<float2 *>(o + 5) = make_float2(v[5], v[6]);
+        *reinterpret_cast<float2 *>(o + 7) = make_float2(v[7], v[8]);
+    } else {
+        *reinterpret_cast<float2 *>(o) = make_float2(v[0], v[1]);
+        *reinterpret_cast<float2 *>(o + 2) = make_float2(v[2], v[3]);
+        *reinterpret_cast<float2 *>(o + 4) = make_float2(v[4], v[5]);
+        *reinterpret_cast<float2 *>(o + 6) = make_float2(v[6], v[7]);
+        o[8] = v[8];
+    }
+}
+
+// The same for a 3x3 FP64 block (72 bytes, 8-byte aligned): four 16-byte
+// stores and one 8-byte store.
+__device__ __forceinline__ void store_block9(double *base, size_t p, const double v[9]) {
+    double *o = base + p * 9;
+    if (reinterpret_cast<uintptr_t>(o) & 15u) {
+        o[0] = v[0];
+        *reinterpret_cast<double2 *>(o + 1) = make_double2(v[1], v[2]);
+        *reinterpret_cast<double2 *>(o + 3) = make_double2(v[3], v[4]);
+        *reinterpret_cast<double2 *>(o + 5) = make_double2(v[5], v[6]);
+        *reinterpret_cast<double2 *>(o + 7) = make_double2(v[7], v[8]);
+    } else {
+        *reinterpret_cast<double2 *>(o) = make_double2(v[0], v[1]);
+        *reinterpret_cast<double2 *>(o + 2) = make_double2(v[2], v[3]);
+        *reinterpret_cast<double2 *>(o + 4) = make_double2(v[4], v[5]);
+        *reinterpret_cast<double2 *>(o + 6) = make_double2(v[6], v[7]);
+        o[8] = v[8];
+    }
+}
+
 // Symmetric diagonal block (j, j): six distinct values d00, d11, d22, d01, d02, d12.
 __device__ __forceinline__ void ela_diag_accumulate(Kahan *acc, float4 g, float B, float mu) {
     const float bx = g.x * B, by = g.y * B, bz = g.z * B;
@@ -278,15 +317,10 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 float v[9];
 #pragma unroll
                 for (int m = 0; m < 9; m++) v[m] = n ? acc[m].value() : 0.f;
-                float *o = values + (size_t)ent.x * 9;
-#pragma unroll
-                for (int m = 0; m < 9; m++) o[m] = v[m];
+                store_block9(values, (size_t)ent.x, v);
                 if (ent.y >= 0) {
-                    float *tr = values + (size_t)ent.y * 9;
-#pragma unroll
-                    for (int a = 0; a < 3; a++)
-#pragma unroll
-                        for (int bb = 0; bb < 3; bb++) tr[3 * bb + a] = v[3 * a + bb];
+                    const float tr[9] = {v[0], v[3], v[6], v[1], v[4], v[7], v[2], v[5], v[8]};
+                    store_block9(values, (size_t)ent.y, tr);
                 }
             }
         }
@@ -348,10 +382,8 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                     d[m] = sv[m];
                 }
                 if (p >= 0) {
-                    float *v = values + (size_t)p * 9;
-                    v[0] = sv[0]; v[1] = sv[3]; v[2] = sv[4];
-                    v[3] = sv[3]; v[4] = sv[1]; v[5] = sv[5];
-                    v[6] = sv[4]; v[7] = sv[5]; v[8] = sv[2];
+                    const float v[9] = {sv[0], sv[3], sv[4], sv[3], sv[1], sv[5], sv[4], sv[5], sv[2]};
+                    store_block9(values, (size_t)p, v);
                 }
                 if (PREC) {
                     if (M.mask) {
@@ -366,10 +398,8 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                     double x[6];
 #pragma unroll
                     for (int m = 0; m < 6; m++) x[m] = f32_to_f64(d[m]);
-                    double *o = precOut + (size_t)r * 9;   // 72-byte blocks: 8-byte aligned
-                    o[0] = x[0]; o[1] = x[3]; o[2] = x[4];
-                    o[3] = x[3]; o[4] = x[1]; o[5] = x[5];
-                    o[6] = x[4]; o[7] = x[5]; o[8] = x[2];
+                    const double o[9] = {x[0], x[3], x[4], x[3], x[1], x[5], x[4], x[5], x[2]};
+                    store_block9(precOut, (size_t)r, o);
                 }
             }
         }
