@@ -47,6 +47,15 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
         : "memory");
 }
 
+// 8-byte asynchronous global -> shared copy (both addresses 8-byte aligned)
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 // error-free sum of two Kahan partials (value = s - c)
 __device__ __forceinline__ void kahan_merge(Kahan &a, float s2, float c2) {
     const float s = a.s + s2;
@@ -210,8 +219,23 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         if (bd) bulk_g2s(sDiag, P.diagEnt + T.diagBegin, bd, bar);
     }
 
-    // 1a. the tile's node coordinates (hi and lo parts) into the contribution
+    // 1a. the weights of set 0 go to shared memory by asynchronous copies
+    //     (cp.async, no register round trip); the connectivity of a thread's
+    //     first two elements is loaded into registers; meanwhile the tile's node
+    //     coordinates (hi and lo parts) are gathered into the contribution
     //     region, which the contribution lists fill only after phase 1
+    const int i0 = tid, i1 = tid + kTileThreads;
+    ushort4 lc0 = make_ushort4(0, 0, 0, 0), lc1 = lc0;
+    if (i0 < T.nElem) {
+        lc0 = P.lconn[T.elemBegin + i0];
+        cp_async8(W + i0, S.w + P.elems[T.elemBegin + i0]);
+    }
+    if (i1 < T.nElem) {
+        lc1 = P.lconn[T.elemBegin + i1];
+        cp_async8(W + i1, S.w + P.elems[T.elemBegin + i1]);
+    }
+    for (int i = i1 + kTileThreads; i < T.nElem; i += kTileThreads)
+        cp_async8(W + i, S.w + P.elems[T.elemBegin + i]);
     float4 *Xh = reinterpret_cast<float4 *>(sm + L.contrib);
     float4 *Xl = Xh + T.nNodes;
     for (int i = tid; i < T.nNodes; i += kTileThreads) {
@@ -219,25 +243,13 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         Xh[i] = M.hl[2 * n];
         Xl[i] = M.hl[2 * n + 1];
     }
-    // the first element's connectivity and weights load meanwhile
-    ushort4 lc = make_ushort4(0, 0, 0, 0);
-    float2 w = make_float2(0.f, 0.f);
-    if (tid < T.nElem) {
-        lc = P.lconn[T.elemBegin + tid];
-        w = S.w[P.elems[T.elemBegin + tid]];
-    }
+    cp_async_wait_all();
     __syncthreads();
 
-    // 1b. gradients of the tile's elements and the weights of set 0
+    // 1b. gradients of the tile's elements
     int flagged = 0;
     for (int i = tid; i < T.nElem; i += kTileThreads) {
-        const int inext = i + kTileThreads;
-        ushort4 lcn = lc;
-        float2 wn = w;
-        if (inext < T.nElem) {
-            lcn = P.lconn[T.elemBegin + inext];
-            wn = S.w[P.elems[T.elemBegin + inext]];
-        }
+        const ushort4 lc = i == i0 ? lc0 : i == i1 ? lc1 : P.lconn[T.elemBegin + i];
         ElemCoords C;
         C.h0 = Xh[lc.x]; C.h1 = Xh[lc.y]; C.h2 = Xh[lc.z]; C.h3 = Xh[lc.w];
         C.l0 = Xl[lc.x]; C.l1 = Xl[lc.y]; C.l2 = Xl[lc.z]; C.l3 = Xl[lc.w];
@@ -249,9 +261,6 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         }
 #pragma unroll
         for (int j = 0; j < 4; j++) G[4 * i + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
-        W[i] = w;
-        lc = lcn;
-        w = wn;
     }
     if (flagged) atomicAdd(counters + 1, flagged);
     __syncthreads();
