@@ -56,6 +56,12 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// Slot of gradient j of tile element l in the gradient array (four 16-byte
+// slots per element, rotated by l / 2): the eight lanes of a quarter warp that
+// store gradient j of eight consecutive elements hit eight distinct bank
+// groups instead of two.
+__device__ __forceinline__ int gslot(int l, int j) { return 4 * l + ((j + (l >> 1)) & 3); }
+
 // error-free sum of two Kahan partials (value = s - c)
 __device__ __forceinline__ void kahan_merge(Kahan &a, float s2, float c2) {
     const float s = a.s + s2;
@@ -267,7 +273,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
             flagged++;
         }
 #pragma unroll
-        for (int j = 0; j < 4; j++) G[4 * i + j] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
+        for (int j = 0; j < 4; j++) G[gslot(i, j)] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
     }
     if (flagged) atomicAdd(counters + 1, flagged);
     __syncthreads();
@@ -314,7 +320,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 for (int q = b; q < b + n; q++) {
                     const unsigned u = sC[q];
                     const int l = u >> 4;
-                    const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
+                    const float4 gj = G[gslot(l, (u >> 2) & 3)], gk = G[gslot(l, u & 3)];
                     const float x = W[l].x * fmaf(gj.x, gk.x, fmaf(gj.y, gk.y, gj.z * gk.z));
                     if (q == b) { acc.s = x; acc.c = 0.f; } else acc.add(x);
                 }
@@ -326,7 +332,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 for (int q = b; q < b + n; q++) {
                     const unsigned u = sC[q];
                     const int l = u >> 4;
-                    const float4 gj = G[4 * l + ((u >> 2) & 3)], gk = G[4 * l + (u & 3)];
+                    const float4 gj = G[gslot(l, (u >> 2) & 3)], gk = G[gslot(l, u & 3)];
                     const float2 w = W[l];
                     ela_accumulate(acc, gj, gk, w.x, w.y, q == b);
                 }
@@ -353,7 +359,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 for (int q = b + part; q < b + n; q += 4) {
                     const unsigned u = sC[q];
                     const int l = u >> 4;
-                    const float4 g = G[4 * l + ((u >> 2) & 3)];
+                    const float4 g = G[gslot(l, (u >> 2) & 3)];
                     acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
                 }
                 quad_combine(acc);
@@ -367,7 +373,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                     const unsigned u = sC[q];
                     const int l = u >> 4;
                     const float2 w = W[l];
-                    ela_diag_accumulate(acc, G[4 * l + ((u >> 2) & 3)], w.x, w.y);
+                    ela_diag_accumulate(acc, G[gslot(l, (u >> 2) & 3)], w.x, w.y);
                 }
 #pragma unroll
                 for (int m = 0; m < 6; m++) quad_combine(acc[m]);
