@@ -215,7 +215,6 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     unsigned short *sC = reinterpret_cast<unsigned short *>(sm + L.contrib);
     int4 *sOff = reinterpret_cast<int4 *>(sm + L.off);
     int2 *sDiag = reinterpret_cast<int2 *>(sm + L.diag);
-    float *sRes = reinterpret_cast<float *>(sm + L.res);              // 12 floats per row
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);           // two barriers
     const int tid = threadIdx.x;
 
@@ -347,13 +346,20 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
             }
         }
 
-        // 3a. diagonal entries: four lanes per row, combined without error
+        // 3. diagonal entries: four lanes per row sum a quarter of the row's
+        //    contributions each and combine them without error; the first lane
+        //    writes the block and its preconditioner block (inverted in FP32,
+        //    stored as FP64)
         const int part = tid & 3;
         for (int base = 0; base < T.nRows; base += kTileThreads / 4) {
             const int rl = base + (tid >> 2);
             const bool active = rl < T.nRows;
             const int2 de = active ? sDiag[rl] : make_int2(0, 0);
             const int b = (unsigned)de.y >> 8, n = de.y & 0xff;
+            const bool writer = active && part == 0;
+            const int r = de.x;
+            const int p = writer ? M.diagPos[r] : -1;
+            const unsigned mk = (PREC && writer && M.mask) ? M.mask[r] : 0u;
             if (OP == MFEM_OP_LAP) {
                 Kahan acc;
                 for (int q = b + part; q < b + n; q += 4) {
@@ -363,9 +369,10 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                     acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
                 }
                 quad_combine(acc);
-                if (active && part == 0) {
-                    sRes[12 * rl] = acc.s;
-                    sRes[12 * rl + 1] = acc.c;
+                if (writer) {
+                    const float v = acc.value();
+                    if (p >= 0) values[p] = v;
+                    if (PREC) precOut[r] = f32_to_f64(1.0f / v);
                 }
             } else {
                 Kahan acc[6];
@@ -377,51 +384,30 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 }
 #pragma unroll
                 for (int m = 0; m < 6; m++) quad_combine(acc[m]);
-                if (active && part == 0) {
+                if (writer) {
+                    float sv[6], d[6];
 #pragma unroll
                     for (int m = 0; m < 6; m++) {
-                        sRes[12 * rl + 2 * m] = acc[m].s;
-                        sRes[12 * rl + 2 * m + 1] = acc[m].c;
+                        sv[m] = acc[m].value();
+                        d[m] = sv[m];
                     }
-                }
-            }
-        }
-        __syncthreads();
-        // 3b. one thread per row: write the diagonal block and the preconditioner
-        //     (inverted in FP32, stored as FP64)
-        for (int rl = tid; rl < T.nRows; rl += kTileThreads) {
-            const int r = sDiag[rl].x;
-            const int p = M.diagPos[r];
-            if (OP == MFEM_OP_LAP) {
-                const float s = sRes[12 * rl], c = sRes[12 * rl + 1];
-                if (p >= 0) values[p] = s - c;
-                if (PREC) precOut[r] = f32_to_f64(1.0f / (s - c));
-            } else {
-                float sv[6], d[6];
-#pragma unroll
-                for (int m = 0; m < 6; m++) {
-                    sv[m] = sRes[12 * rl + 2 * m] - sRes[12 * rl + 2 * m + 1];
-                    d[m] = sv[m];
-                }
-                if (p >= 0) {
-                    const float v[9] = {sv[0], sv[3], sv[4], sv[3], sv[1], sv[5], sv[4], sv[5], sv[2]};
-                    store_block9(values, (size_t)p, v);
-                }
-                if (PREC) {
-                    if (M.mask) {
+                    if (p >= 0) {
+                        const float v[9] = {sv[0], sv[3], sv[4], sv[3], sv[1], sv[5], sv[4], sv[5], sv[2]};
+                        store_block9(values, (size_t)p, v);
+                    }
+                    if (PREC) {
                         // src/Fortran/elasclpr.f:19-27: constrained DOF k -> row and
                         // column k of the block zero, diagonal 1
-                        const unsigned mk = M.mask[r];
                         if (mk & 1u) { d[0] = 1.f; d[3] = 0.f; d[4] = 0.f; }
                         if (mk & 2u) { d[1] = 1.f; d[3] = 0.f; d[5] = 0.f; }
                         if (mk & 4u) { d[2] = 1.f; d[4] = 0.f; d[5] = 0.f; }
-                    }
-                    if (p >= 0 && !inv3_sym32(d)) atomicAdd(counters, 1);
-                    double x[6];
+                        if (p >= 0 && !inv3_sym32(d)) atomicAdd(counters, 1);
+                        double x[6];
 #pragma unroll
-                    for (int m = 0; m < 6; m++) x[m] = f32_to_f64(d[m]);
-                    const double o[9] = {x[0], x[3], x[4], x[3], x[1], x[5], x[4], x[5], x[2]};
-                    store_block9(precOut, (size_t)r, o);
+                        for (int m = 0; m < 6; m++) x[m] = f32_to_f64(d[m]);
+                        const double o[9] = {x[0], x[3], x[4], x[3], x[1], x[5], x[4], x[5], x[2]};
+                        store_block9(precOut, (size_t)r, o);
+                    }
                 }
             }
         }

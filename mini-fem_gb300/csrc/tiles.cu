@@ -14,10 +14,10 @@
 //      mbarrier) over the node coordinates, which are no longer needed;
 //   2. one thread per off-diagonal entry sums its contributions with Kahan
 //      compensation and writes the 3x3 block (or scalar) to the CSR values;
-//   3. four lanes per diagonal entry sum a quarter of its contributions each,
-//      combine them with error-free additions, write the block, and -- on the
-//      FP64 pipe, beside the other warps' FP32 and memory work -- mask and invert
-//      it into the preconditioner.
+//   3. four lanes per diagonal entry sum a quarter of its contributions each
+//      and combine them with error-free additions; the first of the four writes
+//      the block, masks it and inverts it in FP32 (power-of-two scaled
+//      cofactors) into the FP64 preconditioner.
 // The plan is built once per mesh on the host from the device pattern.  Every
 // contribution list is in ascending element order and every combination order
 // is fixed, so results are deterministic.
@@ -83,8 +83,7 @@ SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRow
     L.contrib = L.w + round_up(maxElem * 8, 16);        // weights: float2 per element
     L.off = L.contrib + round_up(std::max(maxContribPad * 2, maxNodes * 32), 16);
     L.diag = L.off + maxOffPad * 16;
-    L.res = L.diag + maxRowsPad * 8;
-    L.bar = L.res + round_up(maxRowsPad * 48, 16);      // 12 floats per row
+    L.bar = L.diag + maxRowsPad * 8;
     L.bytes = L.bar + 16;                               // two mbarriers
     return L;
 }

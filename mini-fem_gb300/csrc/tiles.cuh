@@ -66,7 +66,7 @@ struct TileCtl {
 // holds the tile's node coordinates (32 bytes per node) while the gradients are
 // computed, then the contribution lists.
 struct SmemLayout {
-    int w, contrib, off, diag, res, bar, bytes;
+    int w, contrib, off, diag, bar, bytes;
 };
 
 SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes);
