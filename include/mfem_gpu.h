@@ -40,7 +40,10 @@ extern "C" {
 /* precision */
 #define MFEM_FP64 0   /* FP64 arithmetic and values */
 #define MFEM_FP32 1   /* FP32 element arithmetic and values, compensated sums,
-                         FP64 for flagged slivers and the block inversion */
+                         FP64 gradients for flagged slivers; preconditioner
+                         blocks inverted from the compensated diagonal sums
+                         (tile kernel: FP32 cofactors of the power-of-two scaled
+                         block; record kernel: FP64) and stored as FP64 */
 
 /* strategy */
 #define MFEM_AUTO    (-1)
