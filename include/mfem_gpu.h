@@ -166,6 +166,27 @@ int mfem_profile_read(mfem_context *ctx, char *names, int namesCap, float *ms, i
 int mfem_get_sizes(mfem_context *ctx, int *nbElem, int *nbNodes, int *nbEdges,
                    int *nbColors);
 
+/* ---- pipelined steps ---------------------------------------------------------- */
+/* One iteration of the reference's FEM loop (src/FEM.cc:177-234: assembly,
+ * prec_init, prec_inversion) with host inputs and host outputs, pipelined: no
+ * reference counterpart (its loop is synchronous).  Copies the step's inputs in
+ * (coord: nbNodes*3, coef: as mfem_set_coefficients; NULL keeps the current
+ * ones), assembles (and, with prec != NULL, the preconditioner) into one of two
+ * device result slots, and starts copying the results out into values
+ * (nbEdges*opDim floats for MFEM_FP32, doubles for MFEM_FP64) and prec
+ * (nbNodes*opDim doubles) on a second stream, then returns a ticket without
+ * waiting.  So the copy-out of step k overlaps the copy-in and the assembly of
+ * step k+1; a step only waits, on the device, for the copy-out of the step two
+ * before it (same slot).  The host buffers of a step must stay untouched until
+ * mfem_wait(ticket) returns; page-locked (pinned) buffers make the copies
+ * asynchronous.  mfem_wait reports a bounded-wait timeout of that step as
+ * MFEM_ERR_TIMEOUT; wait for tickets in order (a slot is reused every two
+ * steps).  After mfem_wait the synchronous getters read the latest step. */
+int mfem_step_async(mfem_context *ctx, int operatorID, int precision, int strategy,
+                    const double *coord, const double *coef, void *values, double *prec,
+                    long long *ticket);
+int mfem_wait(mfem_context *ctx, long long ticket);
+
 /* ---- allocation-free assembly ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory while they assemble -- code recorded into a CUDA graph by stream

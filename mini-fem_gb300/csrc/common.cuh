@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <string>
 #include <stdexcept>
+#include <utility>
 
 #include "mfem_gpu.h"
 
@@ -55,6 +56,10 @@ struct DevBuf {
         return ptr;
     }
     template <class T> T *as() const { return static_cast<T *>(ptr); }
+    void swap(DevBuf &o) {
+        std::swap(ptr, o.ptr);
+        std::swap(bytes, o.bytes);
+    }
 };
 
 inline unsigned blocks_for(long long n, int threads) {

@@ -146,6 +146,19 @@ void upload_coords(Context &c, const double *coord) {
     c.hasCoords = true;
 }
 
+void upload_coefficients(Context &c, int op, const double *coef) {
+    require_mesh(c);
+    MFEM_REQUIRE(op == MFEM_OP_LAP || op == MFEM_OP_ELA, MFEM_ERR_INVALID_ARG, "operatorID must be 0 or 1");
+    if (!coef) {
+        c.coefOp = -1;
+        return;
+    }
+    const size_t n = (size_t)c.nbElem * (op == MFEM_OP_LAP ? 1 : 2);
+    double *d = (double *)c.coef.reserve(sizeof(double) * n);
+    MFEM_CUDA(cudaMemcpyAsync(d, coef, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+    c.coefOp = op;
+}
+
 void download_col(Context &c, int *col) {
     int *tmp = (int *)c.scratch.reserve(sizeof(int) * (size_t)c.nnz);
     k_plus_one<<<blocks_for(c.nnz, 256), 256, 0, c.stream>>>(c.col.as<int>(), tmp, c.nnz);
@@ -154,6 +167,7 @@ void download_col(Context &c, int *col) {
 }
 
 void assemble(Context &c, int op, int precision, int strategy, bool fusePrec) {
+    pipeline_guard(c);
     require_pattern(c);
     MFEM_REQUIRE(c.hasCoords, MFEM_ERR_STATE, "no coordinates (mfem_update_coords first)");
     MFEM_REQUIRE(op == MFEM_OP_LAP || op == MFEM_OP_ELA, MFEM_ERR_INVALID_ARG, "operatorID must be 0 or 1");
@@ -183,6 +197,86 @@ int guarded(mfem_context *ctx, F &&f) {
     } catch (const std::bad_alloc &) {
         ctx->c.lastError = "host allocation failed";
         return MFEM_ERR_CAPACITY;
+    }
+}
+
+}  // namespace
+
+Pipeline::~Pipeline() {
+    if (copy) cudaStreamSynchronize(copy);
+    for (auto &e : copied)
+        if (e) cudaEventDestroy(e);
+    if (computed) cudaEventDestroy(computed);
+    if (copy) cudaStreamDestroy(copy);
+    if (hostStatus) cudaFreeHost(hostStatus);
+}
+
+// Anything that writes the current result slot first waits (on the device) for
+// the slot's pending copy-out.
+void pipeline_guard(Context &c) {
+    if (c.pipe && c.pipe->recorded[c.pipe->cur])
+        MFEM_CUDA(cudaStreamWaitEvent(c.stream, c.pipe->copied[c.pipe->cur], 0));
+}
+
+namespace {
+
+Pipeline &pipeline(Context &c) {
+    if (!c.pipe) {
+        auto p = std::make_unique<Pipeline>();
+        MFEM_CUDA(cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking));
+        MFEM_CUDA(cudaEventCreateWithFlags(&p->computed, cudaEventDisableTiming));
+        for (auto &e : p->copied) MFEM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        MFEM_CUDA(cudaMallocHost(&p->hostStatus, sizeof(int) * 16));
+        for (int i = 0; i < 16; i++) p->hostStatus[i] = 0;
+        c.pipe = std::move(p);
+    }
+    return *c.pipe;
+}
+
+// One pipelined step (mfem_step_async).
+long long step_async(Context &c, int op, int precision, int strategy, const double *coord,
+                     const double *coef, void *hostValues, double *hostPrec) {
+    require_pattern(c);
+    MFEM_REQUIRE(hostValues, MFEM_ERR_INVALID_ARG, "null host values");
+    Pipeline &P = pipeline(c);
+    const long long t = P.next;
+    if (t > 0) {
+        // the other slot becomes current; the previous step's results stay in
+        // the spare slot while they are copied out
+        c.values.swap(P.spareValues);
+        c.prec.swap(P.sparePrec);
+        P.cur ^= 1;
+    }
+    if (coord) upload_coords(c, coord);
+    if (coef) upload_coefficients(c, op, coef);
+    assemble(c, op, precision, strategy, hostPrec != nullptr);   // waits for the slot's last copy-out
+    int *hs = P.hostStatus + 8 * P.cur;
+    MFEM_CUDA(cudaMemcpyAsync(hs, status_ptr(c), sizeof(int) * 8, cudaMemcpyDeviceToHost, c.stream));
+    MFEM_CUDA(cudaEventRecord(P.computed, c.stream));
+    MFEM_CUDA(cudaStreamWaitEvent(P.copy, P.computed, 0));
+    const size_t n = (size_t)c.nnz * op_dim(op);
+    MFEM_CUDA(cudaMemcpyAsync(hostValues, c.values.ptr, n * (precision == MFEM_FP32 ? 4 : 8),
+                              cudaMemcpyDeviceToHost, P.copy));
+    if (hostPrec)
+        MFEM_CUDA(cudaMemcpyAsync(hostPrec, c.prec.ptr, sizeof(double) * (size_t)c.nbNodes * op_dim(op),
+                                  cudaMemcpyDeviceToHost, P.copy));
+    MFEM_CUDA(cudaEventRecord(P.copied[P.cur], P.copy));
+    P.recorded[P.cur] = true;
+    P.next = t + 1;
+    return t;
+}
+
+void wait_step(Context &c, long long ticket) {
+    MFEM_REQUIRE(c.pipe && ticket >= 0 && ticket < c.pipe->next, MFEM_ERR_INVALID_ARG, "unknown ticket");
+    Pipeline &P = *c.pipe;
+    // the slot's event was recorded by this step or by a later one (stream order)
+    const int slot = (P.cur + (int)((P.next - 1 - ticket) & 1)) & 1;
+    MFEM_CUDA(cudaEventSynchronize(P.copied[slot]));
+    const int *hs = P.hostStatus + 8 * slot;
+    if (hs[6]) {
+        MFEM_CUDA(cudaMemsetAsync(status_ptr(c) + 6, 0, sizeof(int), c.stream));
+        throw Error(MFEM_ERR_TIMEOUT, "a device wait gave up (staged copies did not arrive in time); "
+                                      "the results of that step are incomplete");
     }
 }
 
@@ -330,19 +424,7 @@ int mfem_coloring_creation(mfem_context *ctx, unsigned long long seed, int *colo
 }
 
 int mfem_set_coefficients(mfem_context *ctx, int operatorID, const double *coef) {
-    return mfem::guarded(ctx, [&](Context &c) {
-        mfem::require_mesh(c);
-        MFEM_REQUIRE(operatorID == MFEM_OP_LAP || operatorID == MFEM_OP_ELA, MFEM_ERR_INVALID_ARG,
-                     "operatorID must be 0 or 1");
-        if (!coef) {
-            c.coefOp = -1;
-            return;
-        }
-        const size_t n = (size_t)c.nbElem * (operatorID == MFEM_OP_LAP ? 1 : 2);
-        double *d = (double *)c.coef.reserve(sizeof(double) * n);
-        MFEM_CUDA(cudaMemcpyAsync(d, coef, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
-        c.coefOp = operatorID;
-    });
+    return mfem::guarded(ctx, [&](Context &c) { mfem::upload_coefficients(c, operatorID, coef); });
 }
 
 int mfem_assemble(mfem_context *ctx, int operatorID, int precision, int strategy) {
@@ -379,6 +461,7 @@ int mfem_prec_init(mfem_context *ctx) {
     return mfem::guarded(ctx, [&](Context &c) {
         mfem::require_pattern(c);
         MFEM_REQUIRE(c.lastOp >= 0, MFEM_ERR_STATE, "prec_init before assembly");
+        mfem::pipeline_guard(c);
         mfem::prec_init_fp64(c, c.lastOp);
         c.precIsInit = false;
     });
@@ -388,6 +471,7 @@ int mfem_prec_inversion(mfem_context *ctx, int *nbSingular) {
     return mfem::guarded(ctx, [&](Context &c) {
         mfem::require_pattern(c);
         MFEM_REQUIRE(c.lastOp >= 0 && c.prec.ptr, MFEM_ERR_STATE, "prec_inversion before prec_init");
+        mfem::pipeline_guard(c);
         int s = mfem::prec_invert(c, c.lastOp);
         if (nbSingular) *nbSingular = s;
         c.precIsInit = true;
@@ -590,6 +674,7 @@ int mfem_prec_init_host(mfem_context *ctx, double *prec, double *nodeToNodeValue
         MFEM_REQUIRE(operatorDim == 1 || operatorDim == 9, MFEM_ERR_INVALID_ARG, "operatorDim must be 1 or 9");
         // the values the caller holds are the source (they may have been changed)
         const size_t n = (size_t)c.nnz * operatorDim;
+        mfem::pipeline_guard(c);
         double *dv = (double *)c.values.reserve(sizeof(double) * n);
         MFEM_CUDA(cudaMemcpyAsync(dv, nodeToNodeValue, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
         c.lastOp = op;
@@ -618,6 +703,7 @@ int mfem_prec_inversion_host(mfem_context *ctx, double *prec, int *nodeToNodeRow
             const int rc = mfem_set_check_bounds(ctx, checkBounds);
             if (rc != MFEM_OK) throw Error(rc, c.lastError);
         }
+        mfem::pipeline_guard(c);
         double *dp = (double *)c.prec.reserve(sizeof(double) * (size_t)nbNodes * dim);
         MFEM_CUDA(cudaMemcpyAsync(dp, prec, sizeof(double) * (size_t)nbNodes * dim,
                                   cudaMemcpyHostToDevice, c.stream));
@@ -626,6 +712,19 @@ int mfem_prec_inversion_host(mfem_context *ctx, double *prec, int *nodeToNodeRow
                                   cudaMemcpyDeviceToHost, c.stream));
         MFEM_CUDA(cudaStreamSynchronize(c.stream));
     });
+}
+
+int mfem_step_async(mfem_context *ctx, int operatorID, int precision, int strategy,
+                    const double *coord, const double *coef, void *values, double *prec,
+                    long long *ticket) {
+    return mfem::guarded(ctx, [&](Context &c) {
+        const long long t = mfem::step_async(c, operatorID, precision, strategy, coord, coef, values, prec);
+        if (ticket) *ticket = t;
+    });
+}
+
+int mfem_wait(mfem_context *ctx, long long ticket) {
+    return mfem::guarded(ctx, [&](Context &c) { mfem::wait_step(c, ticket); });
 }
 
 }  // extern "C"

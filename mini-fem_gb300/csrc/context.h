@@ -2,6 +2,7 @@
 // results, all resident in HBM for the lifetime of the context.
 #pragma once
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -62,6 +63,22 @@ struct KernelTimer {
     ~KernelTimer();
 };
 
+// Pipelined end-to-end steps (context.cu: mfem_step_async / mfem_wait): two result slots, so that the
+// copy-out of step k (on its own stream) overlaps the inputs and the assembly
+// of step k+1.  The slot of step k is k & 1; Context::values/prec always hold
+// the slot of the latest step.
+struct Pipeline {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t computed = nullptr;
+    cudaEvent_t copied[2] = {nullptr, nullptr};   // copy-out of the slot finished
+    bool recorded[2] = {false, false};
+    DevBuf spareValues, sparePrec;                // the other slot
+    int cur = 0;                                  // slot now in Context::values
+    int *hostStatus = nullptr;                    // pinned int[2][8]: status per slot
+    long long next = 0;                           // ticket of the next step
+    ~Pipeline();
+};
+
 struct Context {
     int device = 0;
     KernelTimer timer;
@@ -117,6 +134,10 @@ struct Context {
     DevBuf grad;                      // per-element gradient records
     DevBuf scratch, scratch2, scanTmp;
     DevBuf status;                    // int[8] device-side error flags
+
+    // last member: destroyed first, so that its copies finish before the
+    // buffers they read are freed
+    std::unique_ptr<Pipeline> pipe;
 };
 
 // pattern.cu
@@ -140,6 +161,9 @@ void build_coloring(Context &c, unsigned long long seed);
 void assemble_fp64(Context &c, int op, int strategy, bool fusePrec);
 void prec_init_fp64(Context &c, int op);
 int  prec_invert(Context &c, int op);
+
+// context.cu
+void pipeline_guard(Context &c);
 
 // helpers in context.cu
 int *status_ptr(Context &c);

@@ -180,6 +180,34 @@ class Assembler:
         self._check(fn(self._h, op_id(op), _PRECISIONS[precision], _STRATEGIES[strategy]))
         self.op, self.precision = op_id(op), precision
 
+    def step_async(self, op, precision, values, prec=None, coord=None, coef=None,
+                   strategy: str = "gather") -> int:
+        """One pipelined FEM-loop step (mfem_step_async): host inputs in, host
+        results out on a second stream, no wait.  `values` (float32 for fp32,
+        float64 for fp64) and `prec` (float64 or None) must stay alive and
+        untouched until wait(ticket); pinned arrays make the copies asynchronous."""
+        want = np.float32 if precision == "fp32" else np.float64
+        if values.dtype != want or not values.flags.c_contiguous:
+            raise ValueError(f"values must be a contiguous {np.dtype(want).name} array")
+        if values.size != self.nbEdges * op_dim(op):
+            raise ValueError("values has the wrong size")
+        if prec is not None and (prec.dtype != np.float64 or prec.size != self.nbNodes * op_dim(op)
+                                 or not prec.flags.c_contiguous):
+            raise ValueError("prec must be a contiguous float64 array of nbNodes*opDim")
+        for a in (coord, coef):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
+                raise ValueError("coord and coef must be contiguous float64 arrays")
+        t = C.c_longlong()
+        self._check(N.lib.mfem_step_async(
+            self._h, op_id(op), _PRECISIONS[precision], _STRATEGIES[strategy],
+            None if coord is None else _ptr(coord), None if coef is None else _ptr(coef),
+            _ptr(values), None if prec is None else _ptr(prec), C.byref(t)))
+        self.op, self.precision = op_id(op), precision
+        return t.value
+
+    def wait(self, ticket: int):
+        self._check(N.lib.mfem_wait(self._h, ticket))
+
     def prec_init(self):
         self._check(N.lib.mfem_prec_init(self._h))
 
