@@ -7,8 +7,7 @@ jittered, node-permuted Kuhn cube (1,000,000 nodes, 5,821,794 tets,
 A step is one assembly + prec_init + prec_inversion of the whole mesh (what one
 iteration of the reference's FEM loop times, src/FEM.cc:177-234).  `value` is
 the FP32 path (FP32 arithmetic and values, Kahan-compensated sums, FP64
-gradients for slivers, FP32 block inversion stored as FP64) with inputs resident
-in HBM; the plain FP64
+slivers and block inversion) with inputs resident in HBM; the plain FP64
 bit-exact path is reported beside it (`fp64_plain`).  `e2e` runs the same FP32
 step through the C ABI with host buffers: coordinates and coefficients copied
 in, values and preconditioner copied out, every step -- pipelined
@@ -347,7 +346,7 @@ def run_ours(args, rank, world, local_rank):
         "data": "synthetic: jittered (+-0.2h), node-permuted 100^3 Kuhn cube, E log-uniform "
                 "[1e9,2e11], nu U[0.2,0.35], seeded",
         "config": {"workload": workload_name(), "nbElem": E, "nbNodes": N, "nbEdges": nnz,
-                   "operator": "ela", "precision": "fp32 (Kahan sums, fp64 slivers, fp32 block inverse)",
+                   "operator": "ela", "precision": "fp32 (Kahan sums, fp64 slivers + block inverse)",
                    "strategy": "gather", "l2": "flushed (512 MB write) before every timed step",
                    "parallelism": f"replicas x{world}"},
         "roofline": r32, "step_roofline": s32,
@@ -504,7 +503,7 @@ def run_cube30(args, op):
 
 def run_stress(args):
     """60^3 stress cube (1,232,274 tets): jitter 0.45h, 5% slivers, E jump 1e6,
-    nu up to 0.45; FP32 with FP64 slivers and FP32 block inverse against all-FP64."""
+    nu up to 0.45; FP32 with FP64 slivers and block inverse against all-FP64."""
     import torch
     import minifem
     import pyoracle as O
@@ -527,7 +526,7 @@ def run_stress(args):
     v64, p64 = a.values(), a.prec()
     err = metrics.entry_errors(row, col, v64, v32, 9)
     err["preconditioned_operator_rel"] = metrics.operator_error(row, col, v64, p64, v32, p32, 9)
-    return {"metric": "ela stress mesh Melem/s @1.23M tets (FP32, FP64 slivers, FP32 block inverse)",
+    return {"metric": "ela stress mesh Melem/s @1.23M tets (FP32, FP64 slivers + block inverse)",
             "value": round(E / (t32 * 1e-3) / 1e6, 1), "unit": "Melem/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t32, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",

@@ -40,10 +40,7 @@ extern "C" {
 /* precision */
 #define MFEM_FP64 0   /* FP64 arithmetic and values */
 #define MFEM_FP32 1   /* FP32 element arithmetic and values, compensated sums,
-                         FP64 gradients for flagged slivers; preconditioner
-                         blocks inverted from the compensated diagonal sums
-                         (tile kernel: FP32 cofactors of the power-of-two scaled
-                         block; record kernel: FP64) and stored as FP64 */
+                         FP64 for flagged slivers and the block inversion */
 
 /* strategy */
 #define MFEM_AUTO    (-1)

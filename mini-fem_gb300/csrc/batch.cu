@@ -98,7 +98,7 @@ void prepare(mfem_batch &b) {
     MFEM_REQUIRE(!b.items.empty(), MFEM_ERR_STATE, "empty batch");
     // sizes and offsets
     b.totalVal = b.totalPrec = b.totalNodes = 0;
-    int maxW = 0, maxWW = 0, maxC = 0, maxO = 0, maxD = 0;
+    int maxW = 0, maxWW = 0, maxC = 0, maxO = 0, maxD = 0, maxR = 0;
     std::vector<TileDesc> all;
     std::vector<long long> cost;
     size_t maxRec = 0;
@@ -119,7 +119,8 @@ void prepare(mfem_batch &b) {
         maxWW = std::max(maxWW, L.contrib - L.w);
         maxC = std::max(maxC, L.off - L.contrib);
         maxO = std::max(maxO, L.diag - L.off);
-        maxD = std::max(maxD, L.bar - L.diag);
+        maxD = std::max(maxD, L.res - L.diag);
+        maxR = std::max(maxR, L.bar - L.res);
         std::vector<TileDesc> d(c.tiles.nTiles);
         MFEM_CUDA(cudaMemcpy(d.data(), c.tiles.desc.ptr, sizeof(TileDesc) * d.size(), cudaMemcpyDeviceToHost));
         for (auto &t : d) {
@@ -134,7 +135,8 @@ void prepare(mfem_batch &b) {
     L.contrib = L.w + maxWW;
     L.off = L.contrib + maxC;
     L.diag = L.off + maxO;
-    L.bar = L.diag + maxD;
+    L.res = L.diag + maxD;
+    L.bar = L.res + maxR;
     L.bytes = L.bar + 16;
     b.layout = L;
     MFEM_REQUIRE(L.bytes <= 227 * 1024, MFEM_ERR_CAPACITY, "batch: tiles need more than 227 KB");

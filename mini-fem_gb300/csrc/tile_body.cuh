@@ -170,35 +170,56 @@ __device__ __forceinline__ void ela_diag_accumulate(Kahan *acc, float4 g, float 
     acc[5].add(g.y * bz);
 }
 
-// Inverse of a symmetric 3x3 block by its six distinct cofactors in FP32;
+// x * 2^k, exact, by exponent arithmetic on the integer pipe when x and the
+// result are normal; otherwise (zero, subnormal, out of range) by a multiply.
+__device__ __forceinline__ double scale_pow2(double x, int k) {
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e > 0 && e + k > 0 && e + k < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
+    if (x == 0.0) return x;
+    const int kk = max(-1022, min(1023, k));
+    return x * __longlong_as_double((long long)(kk + 1023) << 52);
+}
+
+// 1 / x in FP64: the FP32 reciprocal of x (relative error below 2^-23) refined by
+// two Newton-Raphson steps r <- r + r (1 - x r), each squaring the relative
+// error (2^-46, then below the FP64 rounding): within an ulp or so of the
+// correctly rounded reciprocal, in four FMAs instead of a division.  Values
+// whose FP32 form is not a normal float with a normal reciprocal take the
+// division.
+__device__ __forceinline__ double rcp64(double x) {
+    const double ax = fabs(x);
+    if (!(ax > 0x1.0p-120 && ax < 0x1.0p120)) return 1.0 / x;
+    double r = f32_to_f64(1.0f / f64_to_f32(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+
+// Inverse of a symmetric 3x3 block in FP64 by its six distinct cofactors;
 // d = (d00, d11, d22, d01, d02, d12).  The block is first scaled by the power
-// of two 2^-k that brings its largest diagonal entry to [1, 2) (exact), so that
-// the cofactors (products of two entries) and the determinant (of three) stay
-// inside the FP32 range for any entry magnitude; the inverse of the scaled
-// block times 2^-k is the inverse.  Every cofactor is a 2x2 determinant
-// a*b - c*d evaluated with Kahan's FMA method (within about one ulp), the
-// determinant is their FMA dot product with the first row, and the inverse
-// entries are cofactor * (1 / det): a few ulps relative error per entry for
-// the block given.  Returns false for an exactly singular block, which is then
-// left as it is.
-__device__ __forceinline__ bool inv3_sym32(float d[6]) {
-    const float mx = fmaxf(fabsf(d[0]), fmaxf(fabsf(d[1]), fabsf(d[2])));
-    if (!(mx > 0.f) || mx > 3.0e38f) return false;   // zero, NaN or infinite diagonal
-    const int ex = min(max((int)((__float_as_uint(mx) >> 23) & 0xffu) - 127, -126), 126);
-    const float sc = __uint_as_float((unsigned)(127 - ex) << 23);   // 2^-ex, a normal float
-    const float a = d[0] * sc, e = d[1] * sc, i = d[2] * sc, b = d[3] * sc, c = d[4] * sc,
-                f = d[5] * sc;
-    const float c00 = diff_prod(e, i, f, f);
-    const float c01 = diff_prod(c, f, b, i);
-    const float c02 = diff_prod(b, f, c, e);
-    const float det = fmaf(a, c00, fmaf(b, c01, c * c02));
-    if (det == 0.f) return false;
-    const float r = sc / det;
-    const float c11 = diff_prod(a, i, c, c);
-    const float c12 = diff_prod(b, c, a, f);
-    const float c22 = diff_prod(a, e, b, b);
-    d[0] = c00 * r; d[1] = c11 * r; d[2] = c22 * r;
-    d[3] = c01 * r; d[4] = c02 * r; d[5] = c12 * r;
+// of two 2^-k that brings its largest diagonal entry near 1 (exact, on the
+// integer pipe) so that the determinant's reciprocal can start from FP32; the
+// inverse of the scaled block times 2^-k is the inverse.  Returns false for an
+// exactly singular block, which is then left as it is.
+__device__ __forceinline__ bool inv3_sym(double d[6]) {
+    const double mx = fmax(fabs(d[0]), fmax(fabs(d[1]), fabs(d[2])));
+    if (!(mx > 0.0) || !(mx < INFINITY)) return false;   // zero, NaN or infinite diagonal
+    const int k = (int)((__double_as_longlong(mx) >> 52) & 0x7ff) - 1023;
+    const double a = scale_pow2(d[0], -k), e = scale_pow2(d[1], -k), i = scale_pow2(d[2], -k),
+                 b = scale_pow2(d[3], -k), c = scale_pow2(d[4], -k), f = scale_pow2(d[5], -k);
+    const double c00 = fma(e, i, -f * f);
+    const double c01 = fma(c, f, -b * i);
+    const double c02 = fma(b, f, -c * e);
+    const double det = fma(a, c00, fma(b, c01, c * c02));
+    if (det == 0.0) return false;
+    const double r = rcp64(det);
+    const double c11 = fma(a, i, -c * c);
+    const double c12 = fma(b, c, -a * f);
+    const double c22 = fma(a, e, -b * b);
+    d[0] = scale_pow2(c00 * r, -k); d[1] = scale_pow2(c11 * r, -k); d[2] = scale_pow2(c22 * r, -k);
+    d[3] = scale_pow2(c01 * r, -k); d[4] = scale_pow2(c02 * r, -k); d[5] = scale_pow2(c12 * r, -k);
     return true;
 }
 
@@ -212,11 +233,13 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                                           unsigned char *sm, int *counters, TileCtl ctl) {
     float4 *G = reinterpret_cast<float4 *>(sm);                       // 4 per element
     float2 *W = reinterpret_cast<float2 *>(sm + L.w);                 // (B, mu) or (kappa, -)
+    float *sRes = reinterpret_cast<float *>(sm + L.res);              // kResStride floats per row
     unsigned short *sC = reinterpret_cast<unsigned short *>(sm + L.contrib);
     int4 *sOff = reinterpret_cast<int4 *>(sm + L.off);
     int2 *sDiag = reinterpret_cast<int2 *>(sm + L.diag);
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);           // two barriers
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
+    __shared__ int sNext;   // next off-diagonal unit of phase 2
 
     // 0. stage the entry tables with the TMA engine (barrier 0)
     if (tid == 0) {
@@ -309,9 +332,103 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
             __syncthreads();
         }
 
+        // 3a. diagonal entries: four lanes per row sum a quarter of the row's
+        //     contributions each and combine them without error; the first lane
+        //     writes the block and keeps the compensated sums for 3b
+        const int part = tid & 3;
+        for (int base = 0; base < T.nRows; base += kTileThreads / 4) {
+            const int rl = base + (tid >> 2);
+            const bool active = rl < T.nRows;
+            const int2 de = active ? sDiag[rl] : make_int2(0, 0);
+            const int b = (unsigned)de.y >> 8, n = de.y & 0xff;
+            const bool writer = active && part == 0;
+            const int p = writer ? M.diagPos[de.x] : -1;
+            if (OP == MFEM_OP_LAP) {
+                Kahan acc;
+                for (int q = b + part; q < b + n; q += 4) {
+                    const unsigned u = sC[q];
+                    const int l = u >> 4;
+                    const float4 g = G[gslot(l, (u >> 2) & 3)];
+                    acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
+                }
+                quad_combine(acc);
+                if (writer) {
+                    if (p >= 0) values[p] = acc.value();
+                    if (PREC) {
+                        sRes[kResStride * rl] = acc.s;
+                        sRes[kResStride * rl + 1] = acc.c;
+                    }
+                }
+            } else {
+                Kahan acc[6];
+                for (int q = b + part; q < b + n; q += 4) {
+                    const unsigned u = sC[q];
+                    const int l = u >> 4;
+                    const float2 w = W[l];
+                    ela_diag_accumulate(acc, G[gslot(l, (u >> 2) & 3)], w.x, w.y);
+                }
+#pragma unroll
+                for (int m = 0; m < 6; m++) quad_combine(acc[m]);
+                if (writer) {
+                    float sv[6];
+#pragma unroll
+                    for (int m = 0; m < 6; m++) sv[m] = acc[m].value();
+                    if (p >= 0) {
+                        const float v[9] = {sv[0], sv[3], sv[4], sv[3], sv[1], sv[5], sv[4], sv[5], sv[2]};
+                        store_block9(values, (size_t)p, v);
+                    }
+                    if (PREC) {
+#pragma unroll
+                        for (int m = 0; m < 6; m++) {
+                            sRes[kResStride * rl + 2 * m] = acc[m].s;
+                            sRes[kResStride * rl + 2 * m + 1] = acc[m].c;
+                        }
+                        sRes[kResStride * rl + 12] = __int_as_float(p);
+                    }
+                }
+            }
+        }
+        if (tid == 0) sNext = 0;
+        __syncthreads();   // row sums of 3a and the unit counter are ready
+        if (PREC) {
+            // 3b. one thread per row (full warps on the FP64 pipe): the FP64
+            //     preconditioner block from the compensated sums, while the
+            //     other warps start on phase 2
+            for (int rl = tid; rl < T.nRows; rl += kTileThreads) {
+                const int r = sDiag[rl].x;
+                const float *res = sRes + kResStride * rl;
+                if (OP == MFEM_OP_LAP) {
+                    precOut[r] = rcp64(f32_to_f64(res[0]) - f32_to_f64(res[1]));
+                } else {
+                    double d[6];
+#pragma unroll
+                    for (int m = 0; m < 6; m++) d[m] = f32_to_f64(res[2 * m]) - f32_to_f64(res[2 * m + 1]);
+                    if (M.mask) {
+                        // src/Fortran/elasclpr.f:19-27: constrained DOF k -> row and
+                        // column k of the block zero, diagonal 1
+                        const unsigned mk = M.mask[r];
+                        if (mk & 1u) { d[0] = 1.0; d[3] = 0.0; d[4] = 0.0; }
+                        if (mk & 2u) { d[1] = 1.0; d[3] = 0.0; d[5] = 0.0; }
+                        if (mk & 4u) { d[2] = 1.0; d[4] = 0.0; d[5] = 0.0; }
+                    }
+                    if (__float_as_int(res[12]) >= 0 && !inv3_sym(d)) atomicAdd(counters, 1);
+                    const double o[9] = {d[0], d[3], d[4], d[3], d[1], d[5], d[4], d[5], d[2]};
+                    store_block9(precOut, (size_t)r, o);
+                }
+            }
+        }
+
         // 2. off-diagonal units: entry (r, c) and, when c is a row of this tile,
-        //    its transpose (c, r), which is the same sum transposed
-        for (int t = tid; t < T.nOff; t += kTileThreads) {
+        //    its transpose (c, r), which is the same sum transposed; warps take
+        //    32 units at a time from a shared counter, so that the warps of 3b
+        //    join when their FP64 work is done
+        for (;;) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&sNext, 32);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= T.nOff) break;
+            const int t = base + lane;
+            if (t >= T.nOff) continue;
             const int4 ent = sOff[t];
             const int b = (unsigned)ent.z >> 8, n = ent.z & 0xff;
             if (OP == MFEM_OP_LAP) {
@@ -342,72 +459,6 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 if (ent.y >= 0) {
                     const float tr[9] = {v[0], v[3], v[6], v[1], v[4], v[7], v[2], v[5], v[8]};
                     store_block9(values, (size_t)ent.y, tr);
-                }
-            }
-        }
-
-        // 3. diagonal entries: four lanes per row sum a quarter of the row's
-        //    contributions each and combine them without error; the first lane
-        //    writes the block and its preconditioner block (inverted in FP32,
-        //    stored as FP64)
-        const int part = tid & 3;
-        for (int base = 0; base < T.nRows; base += kTileThreads / 4) {
-            const int rl = base + (tid >> 2);
-            const bool active = rl < T.nRows;
-            const int2 de = active ? sDiag[rl] : make_int2(0, 0);
-            const int b = (unsigned)de.y >> 8, n = de.y & 0xff;
-            const bool writer = active && part == 0;
-            const int r = de.x;
-            const int p = writer ? M.diagPos[r] : -1;
-            const unsigned mk = (PREC && writer && M.mask) ? M.mask[r] : 0u;
-            if (OP == MFEM_OP_LAP) {
-                Kahan acc;
-                for (int q = b + part; q < b + n; q += 4) {
-                    const unsigned u = sC[q];
-                    const int l = u >> 4;
-                    const float4 g = G[gslot(l, (u >> 2) & 3)];
-                    acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
-                }
-                quad_combine(acc);
-                if (writer) {
-                    const float v = acc.value();
-                    if (p >= 0) values[p] = v;
-                    if (PREC) precOut[r] = f32_to_f64(1.0f / v);
-                }
-            } else {
-                Kahan acc[6];
-                for (int q = b + part; q < b + n; q += 4) {
-                    const unsigned u = sC[q];
-                    const int l = u >> 4;
-                    const float2 w = W[l];
-                    ela_diag_accumulate(acc, G[gslot(l, (u >> 2) & 3)], w.x, w.y);
-                }
-#pragma unroll
-                for (int m = 0; m < 6; m++) quad_combine(acc[m]);
-                if (writer) {
-                    float sv[6], d[6];
-#pragma unroll
-                    for (int m = 0; m < 6; m++) {
-                        sv[m] = acc[m].value();
-                        d[m] = sv[m];
-                    }
-                    if (p >= 0) {
-                        const float v[9] = {sv[0], sv[3], sv[4], sv[3], sv[1], sv[5], sv[4], sv[5], sv[2]};
-                        store_block9(values, (size_t)p, v);
-                    }
-                    if (PREC) {
-                        // src/Fortran/elasclpr.f:19-27: constrained DOF k -> row and
-                        // column k of the block zero, diagonal 1
-                        if (mk & 1u) { d[0] = 1.f; d[3] = 0.f; d[4] = 0.f; }
-                        if (mk & 2u) { d[1] = 1.f; d[3] = 0.f; d[5] = 0.f; }
-                        if (mk & 4u) { d[2] = 1.f; d[4] = 0.f; d[5] = 0.f; }
-                        if (p >= 0 && !inv3_sym32(d)) atomicAdd(counters, 1);
-                        double x[6];
-#pragma unroll
-                        for (int m = 0; m < 6; m++) x[m] = f32_to_f64(d[m]);
-                        const double o[9] = {x[0], x[3], x[4], x[3], x[1], x[5], x[4], x[5], x[2]};
-                        store_block9(precOut, (size_t)r, o);
-                    }
                 }
             }
         }

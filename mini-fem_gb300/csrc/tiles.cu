@@ -12,12 +12,15 @@
 //      list) into shared memory: each element once per tile that needs it, no
 //      records in HBM; the contribution lists are then copied (second
 //      mbarrier) over the node coordinates, which are no longer needed;
+//   3a. four lanes per diagonal entry sum a quarter of its contributions each
+//      and combine them with error-free additions; the first of the four writes
+//      the block and keeps the compensated sums;
+//   3b. one thread per row (the first warps) masks the block and inverts it in
+//      FP64 into the preconditioner, while the other warps already run phase 2;
 //   2. one thread per off-diagonal entry sums its contributions with Kahan
 //      compensation and writes the 3x3 block (or scalar) to the CSR values;
-//   3. four lanes per diagonal entry sum a quarter of its contributions each
-//      and combine them with error-free additions; the first of the four writes
-//      the block, masks it and inverts it in FP32 (power-of-two scaled
-//      cofactors) into the FP64 preconditioner.
+//      warps take 32 entries at a time from a shared counter, so that the warps
+//      of 3b join when their FP64 work is done.
 // The plan is built once per mesh on the host from the device pattern.  Every
 // contribution list is in ascending element order and every combination order
 // is fixed, so results are deterministic.
@@ -83,7 +86,8 @@ SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRow
     L.contrib = L.w + round_up(maxElem * 8, 16);        // weights: float2 per element
     L.off = L.contrib + round_up(std::max(maxContribPad * 2, maxNodes * 32), 16);
     L.diag = L.off + maxOffPad * 16;
-    L.bar = L.diag + maxRowsPad * 8;
+    L.res = L.diag + maxRowsPad * 8;
+    L.bar = L.res + round_up(maxRowsPad * 4 * kResStride, 16);
     L.bytes = L.bar + 16;                               // two mbarriers
     return L;
 }

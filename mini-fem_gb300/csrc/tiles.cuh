@@ -7,6 +7,11 @@ namespace mfem {
 
 constexpr int kTileThreads = 256;
 
+// Diagonal rows kept for the preconditioner pass: six (sum, compensation)
+// pairs and the row's diagonal CSR position; 13 words, odd, so that the reads
+// of consecutive rows by a warp hit distinct banks.
+constexpr int kResStride = 13;
+
 // One tile: rows (diagonal table), elements, off-diagonal entries and the
 // contribution lists they reference.  Segment starts are 16-byte aligned and the
 // *Pad counts cover whole 16-byte units, so each segment is one bulk copy.
@@ -66,7 +71,7 @@ struct TileCtl {
 // holds the tile's node coordinates (32 bytes per node) while the gradients are
 // computed, then the contribution lists.
 struct SmemLayout {
-    int w, contrib, off, diag, bar, bytes;
+    int w, contrib, off, diag, res, bar, bytes;
 };
 
 SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes);

@@ -194,7 +194,7 @@ def test_fp32_within_tolerance(gpu, op, n, jit, sliver, kernel, tile):
     assert err.max() < TOL_FP32, err.max()
     if sliver:
         assert a.flagged() > 0
-    # the preconditioner: inverse of the assembled diagonal blocks
+    # the preconditioner: FP64 inverse of the compensated diagonal blocks
     p = a.prec()
     assert np.all(np.isfinite(p))
     rel = np.abs(p - ref["prec"]) / (np.abs(ref["prec"]).reshape(-1, d).max(axis=1).repeat(d) + 1e-300)
