@@ -184,6 +184,28 @@ int mfem_step_async(mfem_context *ctx, int operatorID, int precision, int strate
                     long long *ticket);
 int mfem_wait(mfem_context *ctx, long long ticket);
 
+/* ---- consumer of the assembled system ------------------------------------------ */
+/* No counterpart in the reference, whose driver names the step after assembly
+ * ("assembly, solver & update", src/main.cc:353) without implementing it.  All
+ * three use the latest assembly of the context (FP64 or FP32 values; FP64
+ * vectors and arithmetic).  constrained != 0 applies the check bounds as
+ * homogeneous Dirichlet constraints: a constrained DOF is taken as 0 in every
+ * product and its row is the identity (the operator M A M + I - M, whose
+ * block-Jacobi inverse is the masked, inverted diagonal block that
+ * prec_inversion builds, src/Fortran/elasclpr.f:19-27). */
+/* y = A x; x and y are DEVICE pointers (nbNodes*opDim doubles), enqueued on the
+ * context stream. */
+int mfem_spmv(mfem_context *ctx, const double *x, double *y, int constrained);
+/* z = P r with the block-Jacobi preconditioner; DEVICE pointers. */
+int mfem_prec_apply(mfem_context *ctx, const double *r, double *z);
+/* Solves A x = b by conjugate gradients with the block-Jacobi preconditioner
+ * until ||b - A x|| <= rtol ||b|| or maxIter iterations; b and x are HOST
+ * arrays (x: initial guess in, solution out).  Reductions run in a fixed order:
+ * the same inputs give the same bits.  iters, relres (may be NULL): iterations
+ * done and the final relative residual of the recurrence. */
+int mfem_pcg(mfem_context *ctx, const double *b, double *x, double rtol, int maxIter,
+             int constrained, int *iters, double *relres);
+
 /* ---- allocation-free assembly ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory while they assemble -- code recorded into a CUDA graph by stream

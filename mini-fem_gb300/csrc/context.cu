@@ -727,4 +727,26 @@ int mfem_wait(mfem_context *ctx, long long ticket) {
     return mfem::guarded(ctx, [&](Context &c) { mfem::wait_step(c, ticket); });
 }
 
+int mfem_spmv(mfem_context *ctx, const double *x, double *y, int constrained) {
+    return mfem::guarded(ctx, [&](Context &c) {
+        MFEM_REQUIRE(x && y, MFEM_ERR_INVALID_ARG, "null vector");
+        mfem::spmv_device(c, x, y, constrained);
+    });
+}
+
+int mfem_prec_apply(mfem_context *ctx, const double *r, double *z) {
+    return mfem::guarded(ctx, [&](Context &c) {
+        MFEM_REQUIRE(r && z, MFEM_ERR_INVALID_ARG, "null vector");
+        mfem::prec_apply_device(c, r, z);
+    });
+}
+
+int mfem_pcg(mfem_context *ctx, const double *b, double *x, double rtol, int maxIter, int constrained,
+             int *iters, double *relres) {
+    return mfem::guarded(ctx, [&](Context &c) {
+        mfem::check_async(c);
+        mfem::pcg(c, b, x, rtol, maxIter, constrained, iters, relres);
+    });
+}
+
 }  // extern "C"

@@ -132,6 +132,7 @@ struct Context {
 
     // scratch
     DevBuf grad;                      // per-element gradient records
+    DevBuf solver;                    // CG work vectors (solve.cu)
     DevBuf scratch, scratch2, scanTmp;
     DevBuf status;                    // int[8] device-side error flags
 
@@ -164,6 +165,13 @@ int  prec_invert(Context &c, int op);
 
 // context.cu
 void pipeline_guard(Context &c);
+
+// solve.cu
+int op_dim_of(const Context &c);
+void spmv_device(Context &c, const double *x, double *y, int constrainedFlag);
+void prec_apply_device(Context &c, const double *r, double *z);
+void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int constrainedFlag,
+         int *iters, double *relres);
 
 // helpers in context.cu
 int *status_ptr(Context &c);

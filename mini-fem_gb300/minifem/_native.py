@@ -57,6 +57,9 @@ _SIGS = {
     "mfem_step_async": ([_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp,
                          C.POINTER(C.c_longlong)], C.c_int),
     "mfem_wait": ([_vp, C.c_longlong], C.c_int),
+    "mfem_spmv": ([_vp, _vp, _vp, C.c_int], C.c_int),
+    "mfem_prec_apply": ([_vp, _vp, _vp], C.c_int),
+    "mfem_pcg": ([_vp, _vp, _vp, C.c_double, C.c_int, C.c_int, _ip, C.POINTER(C.c_double)], C.c_int),
     "mfem_profile": ([_vp, C.c_int], C.c_int),
     "mfem_profile_read": ([_vp, C.c_char_p, C.c_int, _fp, C.c_int, _ip], C.c_int),
     "mfem_get_sizes": ([_vp, _ip, _ip, _ip, _ip], C.c_int),

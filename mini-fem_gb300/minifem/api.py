@@ -208,6 +208,25 @@ class Assembler:
     def wait(self, ticket: int):
         self._check(N.lib.mfem_wait(self._h, ticket))
 
+    # -- consumer of the assembled system
+    def spmv(self, x_dev: int, y_dev: int, constrained: bool = False):
+        """y = A x on device pointers (nbNodes*opDim doubles each)."""
+        self._check(N.lib.mfem_spmv(self._h, C.c_void_p(x_dev), C.c_void_p(y_dev), int(constrained)))
+
+    def prec_apply(self, r_dev: int, z_dev: int):
+        self._check(N.lib.mfem_prec_apply(self._h, C.c_void_p(r_dev), C.c_void_p(z_dev)))
+
+    def pcg(self, b, x0=None, rtol: float = 1e-8, max_iter: int = 1000,
+            constrained: bool = True):
+        """Block-Jacobi preconditioned CG on the latest assembly (host arrays);
+        returns (x, iterations, relative residual)."""
+        b = _f64(b)
+        x = np.zeros_like(b) if x0 is None else _f64(x0).copy()
+        it, rel = C.c_int(), C.c_double()
+        self._check(N.lib.mfem_pcg(self._h, _ptr(b), _ptr(x), rtol, max_iter, int(constrained),
+                                   C.byref(it), C.byref(rel)))
+        return x, it.value, rel.value
+
     def prec_init(self):
         self._check(N.lib.mfem_prec_init(self._h))
 
