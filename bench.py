@@ -538,6 +538,58 @@ def run_stress(args):
             "fp32_errors_vs_fp64": err}
 
 
+def run_solve(args):
+    """Consumer of the 100^3 ela assembly: block-CSR SpMV (FP64 and FP32 values,
+    FP64 vectors) with its bytes against the HBM peak, and block-Jacobi PCG to a
+    relative residual of 1e-8 on the Dirichlet-constrained system."""
+    import torch
+    import minifem
+    import pyoracle as O
+    mesh = make_mesh(0)
+    E, N = mesh.nbElem, mesh.nbNodes
+    a = minifem.Assembler(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    nnz = len(col)
+    a.set_coefficients("ela", mesh.coef)
+    a.set_check_bounds(O.checkbounds(mesh.boundNodesCode))
+    stream = torch.cuda.ExternalStream(a.stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    timed = _timer(torch, stream, flush)
+    x = torch.randn(3 * N, dtype=torch.float64, device="cuda:0")
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    hbm, peak_kind = peaks()
+    out = {}
+    b = np.random.default_rng(SEED).standard_normal(3 * N)
+    for prec in ("fp64", "fp32"):
+        a.assembly("ela", prec, "gather", prec=True)
+        a.synchronize()
+        ms = timed(lambda: a.spmv(x.data_ptr(), y.data_ptr(), True), args.steps, args.warmup)
+        w = 8 if prec == "fp64" else 4
+        # values and columns once, row pointers, x once (gathers hit L2), y written
+        byts = nnz * (9 * w + 4) + (N + 1) * 4 + 24 * N + 24 * N + N
+        sol, it, rel = a.pcg(b, rtol=1e-8, max_iter=5000)
+        t0 = time.perf_counter()
+        sol, it, rel = a.pcg(b, rtol=1e-8, max_iter=5000)
+        wall = time.perf_counter() - t0
+        out[prec] = {"spmv_ms": round(ms, 4), "spmv_GBs": round(byts / (ms * 1e-3) / 1e9, 1),
+                     "spmv_hbm_frac": round(byts / (ms * 1e-3) / 1e9 / hbm, 4),
+                     "spmv_bytes": byts, "spmv_fp64_fma": 9 * nnz,
+                     "pcg_iterations": it, "pcg_relres": rel, "pcg_s": round(wall, 4),
+                     "pcg_ms_per_iteration": round(wall * 1e3 / max(it, 1), 4)}
+    return {"metric": "ela 100^3 operator apply GB/s and block-Jacobi PCG (consumer of the assembly)",
+            "value": out["fp32"]["spmv_GBs"], "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["fp32"]["spmv_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 values, f64 vectors",
+            "data": "synthetic 100^3 ela cube as the benchmark line; b seeded N(0,1)",
+            "config": {"workload": "ela_cube100_spmv_pcg", "nbNodes": N, "nbEdges": nnz,
+                       "constrained": "check bounds as homogeneous Dirichlet",
+                       "l2": "flushed before every timed SpMV"},
+            "peak_GBs": hbm, "peak_kind": peak_kind, "fp64_values": out["fp64"],
+            "fp32_values": out["fp32"]}
+
+
 def run_batch(args):
     """64 meshes, n ~ U{12..60} nodes per side (seeded), half lap half ela, 8
     coefficient sets each, re-assembled per iteration by one graph replay."""
@@ -590,7 +642,7 @@ def main():
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--workload", default="ela100",
-                    choices=["ela100", "ela30", "lap30", "stress60", "batch64"],
+                    choices=["ela100", "ela30", "lap30", "stress60", "batch64", "solve100"],
                     help="ela100: the benchmark line; the others: the remaining configurations")
     ap.add_argument("--side", type=int, default=N_SIDE,
                     help="nodes per cube side (100 = the benchmark mesh; smaller for profiling)")
@@ -619,6 +671,8 @@ def main():
             out = run_cube30(args, args.workload[:3])
         elif args.workload == "stress60":
             out = run_stress(args)
+        elif args.workload == "solve100":
+            out = run_solve(args)
         else:
             out = run_batch(args)
         if out is not None:

@@ -96,6 +96,18 @@ __device__ __forceinline__ float f64_to_f32(double x) {
     return __uint_as_float(r);
 }
 
+// float -> double is exact; done with integer operations so that it does not
+// occupy GB300's narrow FP64 pipe (zero and subnormal inputs take the
+// conversion instruction).
+__device__ __forceinline__ double f32_to_f64(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    const unsigned lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 // Weights of the FP32 blocks: (B, mu) = (lambda + mu, mu) for ela, (kappa, 0)
 // for lap, in FP32 from the FP64 per-element coefficients (NULL: the reference
 // constants B = 1.25, mu = 1, kappa = 1).

@@ -17,6 +17,7 @@
 #include <cmath>
 
 #include "context.h"
+#include "elem32.cuh"
 
 namespace mfem {
 
@@ -29,7 +30,7 @@ constexpr int kLanesPerRow = 8;          // SpMV: eight lanes share a block row
 constexpr int kRowsPerCta = kThreads / kLanesPerRow;
 
 __device__ __forceinline__ double to_f64(double v) { return v; }
-__device__ __forceinline__ double to_f64(float v) { return (double)v; }
+__device__ __forceinline__ double to_f64(float v) { return f32_to_f64(v); }
 
 // Tree sum of one value per thread into partial[blockIdx.x] (fixed order).
 __device__ __forceinline__ void cta_sum(double v, double *partial) {
@@ -49,30 +50,48 @@ __device__ __forceinline__ bool constrained(const unsigned char *mask, int node,
     return mask && (dim == 1 ? mask[node] != 0 : ((mask[node] >> k) & 1u));
 }
 
-// y = A x; with `partial`, also the CTA partial sums of x . y.
+// y = A x; with `partial`, also the CTA partial sums of x . y.  Eight lanes
+// share a block row: for every chunk of eight blocks they copy the chunk's
+// values (contiguous in CSR order) into shared memory with coalesced loads,
+// then each lane multiplies one block by its gathered x entries.
 template <typename V, int D>
 __global__ void __launch_bounds__(kThreads)
 k_spmv(const int *__restrict__ rowPtr, const int *__restrict__ col, const V *__restrict__ vals,
        const double *__restrict__ x, double *__restrict__ y, int N,
        const unsigned char *__restrict__ mask, double *__restrict__ partial) {
-    const int row = blockIdx.x * kRowsPerCta + threadIdx.x / kLanesPerRow;
+    constexpr int B = D * D;
+    __shared__ V sv[kRowsPerCta][kLanesPerRow * B];
+    const int g = threadIdx.x / kLanesPerRow;
+    const int row = blockIdx.x * kRowsPerCta + g;
     const int sub = threadIdx.x % kLanesPerRow;
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);   // the eight lanes of this row
     double a[D];
 #pragma unroll
     for (int d = 0; d < D; d++) a[d] = 0.0;
+    int kb = 0, ke = 0;
     if (row < N) {
-        const int e = rowPtr[row + 1];
-        for (int k = rowPtr[row] + sub; k < e; k += kLanesPerRow) {
-            const int c = col[k];
+        kb = rowPtr[row];
+        ke = rowPtr[row + 1];
+    }
+    for (int k0 = kb; k0 < ke; k0 += kLanesPerRow) {
+        const int nb = min(kLanesPerRow, ke - k0);
+        const V *src = vals + (size_t)k0 * B;
+        for (int m = sub; m < nb * B; m += kLanesPerRow) sv[g][m] = src[m];
+        __syncwarp(gmask);
+        if (sub < nb) {
+            const int c = col[k0 + sub];
+            const unsigned mc = mask ? mask[c] : 0u;
             double xc[D];
 #pragma unroll
-            for (int d = 0; d < D; d++) xc[d] = constrained(mask, c, d, D) ? 0.0 : x[(size_t)c * D + d];
-            const V *v = vals + (size_t)k * D * D;
+            for (int d = 0; d < D; d++)
+                xc[d] = (D == 1 ? mc != 0u : ((mc >> d) & 1u)) ? 0.0 : x[(size_t)c * D + d];
+            const V *v = sv[g] + sub * B;
 #pragma unroll
             for (int i = 0; i < D; i++)
 #pragma unroll
                 for (int j = 0; j < D; j++) a[i] = fma(to_f64(v[D * i + j]), xc[j], a[i]);
         }
+        __syncwarp(gmask);
     }
 #pragma unroll
     for (int off = kLanesPerRow / 2; off >= 1; off >>= 1)

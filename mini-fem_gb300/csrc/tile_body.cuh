@@ -80,18 +80,6 @@ __device__ __forceinline__ void quad_combine(Kahan &k) {
     }
 }
 
-// float -> double is exact; done with integer operations so that it does not
-// occupy GB300's narrow FP64 pipe (zero and subnormal inputs take the
-// conversion instruction).
-__device__ __forceinline__ double f32_to_f64(float x) {
-    const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)x;
-    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
-    const unsigned lo = b << 29;
-    return __hiloint2double((int)hi, (int)lo);
-}
-
 // One elasticity contribution (j, k) in the FP32 form
 //   c(a,b) = B gj_a gk_b + delta_ab mu (gj . gk)
 // which is the reference's ((p_aa A + p_bb mu) + p_cc mu), p_ab B with
