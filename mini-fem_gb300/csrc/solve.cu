@@ -26,7 +26,7 @@ int op_dim_of(const Context &c) { return c.lastOp == MFEM_OP_LAP ? 1 : 9; }
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kLanesPerRow = 8;          // SpMV: eight lanes share a block row
+constexpr int kLanesPerRow = 4;          // SpMV: four lanes share a block row (measured best of 2-16)
 constexpr int kRowsPerCta = kThreads / kLanesPerRow;
 
 __device__ __forceinline__ double to_f64(double v) { return v; }
@@ -50,8 +50,8 @@ __device__ __forceinline__ bool constrained(const unsigned char *mask, int node,
     return mask && (dim == 1 ? mask[node] != 0 : ((mask[node] >> k) & 1u));
 }
 
-// y = A x; with `partial`, also the CTA partial sums of x . y.  Eight lanes
-// share a block row: for every chunk of eight blocks they copy the chunk's
+// y = A x; with `partial`, also the CTA partial sums of x . y.  Four lanes
+// share a block row: for every chunk of four blocks they copy the chunk's
 // values (contiguous in CSR order) into shared memory with coalesced loads,
 // then each lane multiplies one block by its gathered x entries.
 template <typename V, int D>
@@ -64,7 +64,7 @@ k_spmv(const int *__restrict__ rowPtr, const int *__restrict__ col, const V *__r
     const int g = threadIdx.x / kLanesPerRow;
     const int row = blockIdx.x * kRowsPerCta + g;
     const int sub = threadIdx.x % kLanesPerRow;
-    const unsigned gmask = 0xffu << (threadIdx.x & 24);   // the eight lanes of this row
+    const unsigned gmask = ((1u << kLanesPerRow) - 1u) << (threadIdx.x & (32 - kLanesPerRow));   // this row's lanes
     double a[D];
 #pragma unroll
     for (int d = 0; d < D; d++) a[d] = 0.0;
