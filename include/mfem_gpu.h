@@ -101,6 +101,16 @@ int mfem_coloring_creation(mfem_context *ctx, unsigned long long seed, int *colo
  * newOfOld[nbNodes], a permutation.  The caller renumbers coord and elemToNode
  * with it and sets the renumbered mesh. */
 int mfem_rcm_permutation(mfem_context *ctx, int *newOfOld);
+/* Locality orderings of the nodes from the coordinates (newOfOld as above):
+ * MFEM_LOCALITY_MORTON -- Z-order of the coordinates (21 bits per axis);
+ * MFEM_LOCALITY_BISECTION -- recursive coordinate bisection at the median of
+ * the longest axis, leaves of at most 64 nodes numbered depth first: the
+ * geometric counterpart of the reference's D&C tree ordering
+ * (src/main.cc:155-206, DC-lib).  Renumbering candidates for the tuner beside
+ * identity and reverse Cuthill-McKee. */
+#define MFEM_LOCALITY_MORTON    1
+#define MFEM_LOCALITY_BISECTION 2
+int mfem_locality_permutation(mfem_context *ctx, int kind, int *newOfOld);
 
 /* ---- assembly: replaces assembly (src/assembly.cc:615-720) ------------------ */
 /* coef == NULL: the reference operator (constants 1 / 2.25, 1.25).  Otherwise

@@ -20,6 +20,7 @@ OP_LAP, OP_ELA = 0, 1
 FP64, FP32 = 0, 1
 AUTO, GATHER, SCATTER, ATOMIC = -1, 0, 1, 2
 ORDER_SORTED, ORDER_REFERENCE = 0, 1
+LOCALITY_MORTON, LOCALITY_BISECTION = 1, 2
 
 _vp, _ip, _dp, _fp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_float)
 
@@ -37,6 +38,7 @@ _SIGS = {
     "mfem_set_pattern": ([_vp, _vp, _vp, C.c_int], C.c_int),
     "mfem_coloring_creation": ([_vp, C.c_ulonglong, _vp, _vp, C.c_int, _ip], C.c_int),
     "mfem_rcm_permutation": ([_vp, _vp], C.c_int),
+    "mfem_locality_permutation": ([_vp, C.c_int, _vp], C.c_int),
     "mfem_set_coefficients": ([_vp, C.c_int, _vp], C.c_int),
     "mfem_assemble": ([_vp, C.c_int, C.c_int, C.c_int], C.c_int),
     "mfem_assemble_prec": ([_vp, C.c_int, C.c_int, C.c_int], C.c_int),

@@ -131,6 +131,14 @@ class Assembler:
         self._check(N.lib.mfem_rcm_permutation(self._h, _ptr(out)))
         return out
 
+    def locality_permutation(self, kind: str = "bisection"):
+        """newOfOld[N]: Morton ("morton") or recursive-coordinate-bisection
+        ("bisection") renumbering of the nodes from their coordinates."""
+        k = {"morton": N.LOCALITY_MORTON, "bisection": N.LOCALITY_BISECTION}[kind]
+        out = np.empty(self.nbNodes, np.int32)
+        self._check(N.lib.mfem_locality_permutation(self._h, k, _ptr(out)))
+        return out
+
     def create_elemToEdge(self):
         out = np.empty(self.nbElem * 16, np.int32)
         self._check(N.lib.mfem_create_elemToEdge(self._h, _ptr(out)))

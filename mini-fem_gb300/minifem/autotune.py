@@ -7,8 +7,9 @@ the only bit-exact one, so a caller that needs bit-exactness keeps it):
   (spatial row tiles, gradients in shared memory) with tile sizes
   (rows, elements) from TILE_CANDIDATES;
 * FP64: strategy gather / atomic / scatter (colour-ordered);
-* node numbering: identity or reverse Cuthill-McKee (the caller applies it, since
-  it renumbers the output).
+* node numbering: identity, reverse Cuthill-McKee, Morton or recursive coordinate
+  bisection (`tune_renumbering`; the caller applies the permutation, since it
+  renumbers the output).
 
 Each candidate runs `repeats` times after one warm-up; the median of the per-step
 device times (CUDA events recorded by the library around its launches) decides.
@@ -93,3 +94,41 @@ def _apply(asm, choice: dict):
     for k in ("fp32_kernel", "tile_rows", "tile_elems"):
         if k in choice:
             asm.set_option(k, choice[k])
+
+
+RENUMBERINGS = ("identity", "rcm", "morton", "bisection")
+
+
+def tune_renumbering(mesh, op: str, precision: str = "fp32", repeats: int = 3, device: int = 0,
+                     candidates=RENUMBERINGS) -> dict:
+    """Time one assembly (+ preconditioner) of `mesh` (a meshgen.Mesh) under each
+    node renumbering and return {"choice", "newOfOld" (None for identity), "ms",
+    "timings"}; every candidate is assembled on its own context."""
+    from .api import Assembler
+    from .meshgen import renumber_nodes
+    base = Assembler(device)
+    base.set_mesh(mesh.coord, mesh.elemToNode)
+    base.create_nodeToNode("sorted")
+    perms = {"identity": None}
+    if "rcm" in candidates:
+        perms["rcm"] = base.rcm_permutation()
+    for kind in ("morton", "bisection"):
+        if kind in candidates:
+            perms[kind] = base.locality_permutation(kind)
+    base.close()
+    timings = []
+    for name in candidates:
+        p = perms[name]
+        m = mesh if p is None else renumber_nodes(mesh, p)
+        a = Assembler(device)
+        try:
+            a.set_mesh(m.coord, m.elemToNode)
+            a.create_nodeToNode("sorted")
+            if m.coef is not None:
+                a.set_coefficients(op, m.coef)
+            timings.append((name, _time(a, op, precision, "gather", repeats)))
+        finally:
+            a.close()
+    choice, ms = min(timings, key=lambda x: x[1])
+    return {"choice": choice, "newOfOld": perms[choice], "ms": ms,
+            "timings": [[n, t] for n, t in timings]}

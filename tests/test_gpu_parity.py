@@ -298,6 +298,48 @@ def test_rcm_renumbering_is_a_permutation_and_exact(gpu):
     assert v[o1].tobytes() == v2[o2].tobytes()
 
 
+@pytest.mark.parametrize("kind", ["morton", "bisection"])
+def test_locality_renumbering_is_a_permutation_and_exact(gpu, kind):
+    """Morton and recursive-bisection orderings: permutations that shrink the
+    bandwidth of the randomly numbered cube; the renumbered mesh assembles to the
+    permuted matrix bit for bit."""
+    from minifem.meshgen import bandwidth, renumber_nodes
+    m = cube_mesh(10, seed=6, op="ela")
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    perm = a.locality_permutation(kind)
+    assert sorted(perm) == list(range(m.nbNodes))
+    r = renumber_nodes(m, perm)
+    assert bandwidth(r.elemToNode) < bandwidth(m.elemToNode) / 2
+    a.set_coefficients("ela", m.coef)
+    a.assembly("ela")
+    v = a.values().reshape(-1, 9)
+    b = gpu(0)
+    b.set_mesh(r.coord, r.elemToNode)
+    row2, col2 = b.create_nodeToNode("sorted")
+    b.set_coefficients("ela", m.coef)
+    b.assembly("ela")
+    v2 = b.values().reshape(-1, 9)
+    rr = np.repeat(np.arange(m.nbNodes), np.diff(row))
+    key_old = perm[rr].astype(np.int64) * m.nbNodes + perm[col - 1]
+    rr2 = np.repeat(np.arange(m.nbNodes), np.diff(row2))
+    key_new = rr2.astype(np.int64) * m.nbNodes + (col2 - 1)
+    o1, o2 = np.argsort(key_old), np.argsort(key_new)
+    assert np.array_equal(key_old[o1], key_new[o2])
+    assert v[o1].tobytes() == v2[o2].tobytes()
+
+
+def test_renumbering_tuner(gpu):
+    from minifem import autotune
+    m = cube_mesh(12, seed=8, op="ela")
+    r = autotune.tune_renumbering(m, "ela", "fp32", repeats=2)
+    assert r["choice"] in autotune.RENUMBERINGS
+    assert [t[0] for t in r["timings"]] == list(autotune.RENUMBERINGS)
+    if r["choice"] != "identity":
+        assert sorted(r["newOfOld"]) == list(range(m.nbNodes))
+
+
 def test_autotuner_picks_a_valid_variant(gpu, tmp_path):
     from minifem import autotune
     m = cube_mesh(12, seed=3, op="ela")
