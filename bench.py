@@ -590,6 +590,30 @@ def run_solve(args):
             "fp32_values": out["fp32"]}
 
 
+def run_renumber(args):
+    """The 100^3 ela cube under each node renumbering the tuner compares:
+    identity (the random numbering of the generator), reverse Cuthill-McKee,
+    Morton and recursive coordinate bisection; FP32 and FP64 steps."""
+    from minifem import autotune
+    mesh = make_mesh(0)
+    E = mesh.nbElem
+    out = {}
+    for prec in ("fp32", "fp64"):
+        r = autotune.tune_renumbering(mesh, "ela", prec, repeats=max(3, args.steps))
+        out[prec] = {"choice": r["choice"],
+                     "ms_per_step": {n: round(t, 4) for n, t in r["timings"]},
+                     "Melem_s": {n: round(E / (t * 1e-3) / 1e6, 1) for n, t in r["timings"]}}
+    best = min(out["fp32"]["ms_per_step"].values())
+    return {"metric": "ela 100^3 Melem/s per node renumbering (tuner candidates)",
+            "value": round(E / (best * 1e-3) / 1e6, 1), "unit": "Melem/s", "n_gpus": 1,
+            "steps": max(3, args.steps), "warmup": 1, "ms_per_step": best, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic 100^3 ela cube as the benchmark line",
+            "config": {"workload": "ela_cube100_renumberings", "timing": "median of the library's "
+                       "per-launch CUDA events, L2 not flushed"},
+            "fp32": out["fp32"], "fp64": out["fp64"]}
+
+
 def run_batch(args):
     """64 meshes, n ~ U{12..60} nodes per side (seeded), half lap half ela, 8
     coefficient sets each, re-assembled per iteration by one graph replay."""
@@ -642,7 +666,8 @@ def main():
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--workload", default="ela100",
-                    choices=["ela100", "ela30", "lap30", "stress60", "batch64", "solve100"],
+                    choices=["ela100", "ela30", "lap30", "stress60", "batch64", "solve100",
+                             "renumber100"],
                     help="ela100: the benchmark line; the others: the remaining configurations")
     ap.add_argument("--side", type=int, default=N_SIDE,
                     help="nodes per cube side (100 = the benchmark mesh; smaller for profiling)")
@@ -673,6 +698,8 @@ def main():
             out = run_stress(args)
         elif args.workload == "solve100":
             out = run_solve(args)
+        elif args.workload == "renumber100":
+            out = run_renumber(args)
         else:
             out = run_batch(args)
         if out is not None:
