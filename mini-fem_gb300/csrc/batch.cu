@@ -2,8 +2,9 @@
 // sets, assembled per iteration by one replay of a CUDA graph.
 //
 // FP32: the graph holds the coordinate splits and ONE persistent launch of the
-// tile kernel over a cross-mesh work list (every tile of every mesh, largest
-// first); CTAs take work items from an atomic counter; each item computes the
+// tile kernel over a cross-mesh work list (every tile of every mesh; meshes
+// largest first, tiles in plan order); CTAs take work items from an atomic
+// counter; each item computes the
 // tile's gradients once and its entries and preconditioner blocks for every
 // coefficient set of its mesh.
 // FP64: the graph holds, per mesh and set, the three bit-exact gather launches
@@ -140,10 +141,15 @@ void prepare(mfem_batch &b) {
     L.bytes = L.bar + 16;
     b.layout = L;
     MFEM_REQUIRE(L.bytes <= 227 * 1024, MFEM_ERR_CAPACITY, "batch: tiles need more than 227 KB");
-    // work list, most expensive first
+    // work list
     std::vector<int> ord(all.size());
     for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
-    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    // meshes by total cost, largest first; a mesh's tiles stay in plan (Morton)
+    // order, which keeps neighbouring tiles' reads and writes close in L2
+    std::vector<long long> meshCost(b.items.size(), 0);
+    for (size_t i = 0; i < all.size(); i++) meshCost[all[i].mesh] += cost[i];
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int x, int y) { return meshCost[all[x].mesh] > meshCost[all[y].mesh]; });
     b.nWork = (int)all.size();
     b.desc.reserve(sizeof(TileDesc) * all.size());
     MFEM_CUDA(cudaMemcpy(b.desc.ptr, all.data(), sizeof(TileDesc) * all.size(), cudaMemcpyHostToDevice));
