@@ -58,7 +58,9 @@ template <typename V, int D>
 __global__ void __launch_bounds__(kThreads)
 k_spmv(const int *__restrict__ rowPtr, const int *__restrict__ col, const V *__restrict__ vals,
        const double *__restrict__ x, double *__restrict__ y, int N,
-       const unsigned char *__restrict__ mask, double *__restrict__ partial) {
+       const unsigned char *__restrict__ mask, double *__restrict__ partial,
+       const int *__restrict__ stop) {
+    if (stop && *stop) return;   // CG: converged in an earlier iteration of the batch
     constexpr int B = D * D;
     __shared__ V sv[kRowsPerCta][kLanesPerRow * B];
     const int g = threadIdx.x / kLanesPerRow;
@@ -128,7 +130,8 @@ __global__ void k_prec_apply(const double *__restrict__ prec, const double *__re
 
 // Scalars of the CG recurrence, kept on the device.
 struct CgScalars {
-    double rz, pq, alpha, beta, rr, bb;
+    double rz, pq, alpha, beta, rr, bb, tol2;
+    int iter, maxIter, stop;   // stop: converged or out of iterations; later kernels do nothing
 };
 
 // r = b - A x (A x already in q); z = P r; partials of r . z, r . r and b . b.
@@ -169,7 +172,8 @@ k_cg_init(const double *__restrict__ prec, const double *__restrict__ b, const d
 
 // Sums `nSums` arrays of nCta partials (in index order) into sums[0..nSums).
 __global__ void k_sum_partials(const double *__restrict__ partial, int nCta, int nSums,
-                               double *__restrict__ sums) {
+                               double *__restrict__ sums, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     __shared__ double s[kThreads];
     for (int k = 0; k < nSums; k++) {
         double t = 0.0;
@@ -185,13 +189,18 @@ __global__ void k_sum_partials(const double *__restrict__ partial, int nCta, int
     }
 }
 
-__global__ void k_cg_start(CgScalars *sc, const double *sums) {
+__global__ void k_cg_start(CgScalars *sc, const double *sums, double tol2, int maxIter) {
     sc->rz = sums[0];
     sc->rr = sums[1];
     sc->bb = sums[2];
+    sc->tol2 = tol2;
+    sc->iter = 0;
+    sc->maxIter = maxIter;
+    sc->stop = (sc->rr <= tol2 * sc->bb || maxIter <= 0) ? 1 : 0;
 }
 
 __global__ void k_cg_alpha(CgScalars *sc, const double *sums) {
+    if (sc->stop) return;
     sc->pq = sums[0];
     sc->alpha = sc->pq != 0.0 ? sc->rz / sc->pq : 0.0;
 }
@@ -203,6 +212,7 @@ k_cg_update(const double *__restrict__ prec, const CgScalars *__restrict__ sc,
             const double *__restrict__ p, const double *__restrict__ q, double *__restrict__ x,
             double *__restrict__ r, double *__restrict__ z, int N, double *__restrict__ partial,
             int nCta) {
+    if (sc->stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double alpha = sc->alpha;
     double rz = 0.0, rr = 0.0;
@@ -232,36 +242,44 @@ k_cg_update(const double *__restrict__ prec, const CgScalars *__restrict__ sc,
 }
 
 __global__ void k_cg_beta(CgScalars *sc, const double *sums) {
+    if (sc->stop) return;
     const double rzNew = sums[0];
     sc->beta = sc->rz != 0.0 ? rzNew / sc->rz : 0.0;
     sc->rz = rzNew;
     sc->rr = sums[1];
+    sc->iter++;
+    if (sc->rr <= sc->tol2 * sc->bb || sc->iter >= sc->maxIter) sc->stop = 1;
 }
 
 // p = z + beta p
 __global__ void k_cg_direction(const CgScalars *__restrict__ sc, const double *__restrict__ z,
                                double *__restrict__ p, long long n) {
+    if (sc->stop) return;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = fma(sc->beta, p[i], z[i]);
 }
 
 template <int D>
 void spmv_t(const Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
-            cudaStream_t s) {
+            const int *stop, cudaStream_t s) {
     const unsigned grid = blocks_for(c.nbNodes, kRowsPerCta);
     if (c.lastPrecision == MFEM_FP32)
         k_spmv<float, D><<<grid, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<float>(),
-                                                   x, y, c.nbNodes, mask, partial);
+                                                   x, y, c.nbNodes, mask, partial, stop);
     else
         k_spmv<double, D><<<grid, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<double>(),
-                                                    x, y, c.nbNodes, mask, partial);
+                                                    x, y, c.nbNodes, mask, partial, stop);
     check_launch("k_spmv");
 }
 
-void spmv(const Context &c, const double *x, double *y, const unsigned char *mask, double *partial) {
-    if (op_dim_of(c) == 9) spmv_t<3>(c, x, y, mask, partial, c.stream);
-    else spmv_t<1>(c, x, y, mask, partial, c.stream);
+void spmv(const Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
+          const int *stop = nullptr) {
+    if (op_dim_of(c) == 9) spmv_t<3>(c, x, y, mask, partial, stop, c.stream);
+    else spmv_t<1>(c, x, y, mask, partial, stop, c.stream);
 }
+
+// CG iterations enqueued between two looks at the convergence flag
+constexpr int kCgBatch = 8;
 
 }  // namespace
 
@@ -304,12 +322,12 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     double *partial = w + 6 * n;
     double *sums = partial + 3 * (size_t)nCta;
     CgScalars *sc = reinterpret_cast<CgScalars *>(sums + 8);
-    double *hostRr = nullptr;
-    MFEM_CUDA(cudaMallocHost(&hostRr, 2 * sizeof(double)));
+    CgScalars *hostSc = nullptr;
+    MFEM_CUDA(cudaMallocHost(&hostSc, sizeof(CgScalars)));
     struct Free {
-        double *p;
+        CgScalars *p;
         ~Free() { cudaFreeHost(p); }
-    } freeHost{hostRr};
+    } freeHost{hostSc};
     const unsigned char *mask = solve_mask(c, constrainedFlag);
     cudaStream_t s = c.stream;
     MFEM_CUDA(cudaMemcpyAsync(vb, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
@@ -320,32 +338,33 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     if (D == 3) k_cg_init<3><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, c.nbNodes, partial, nCtaNodes);
     else k_cg_init<1><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, c.nbNodes, partial, nCtaNodes);
     check_launch("k_cg_init");
-    k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 3, sums);
-    k_cg_start<<<1, 1, 0, s>>>(sc, sums);
-    MFEM_CUDA(cudaMemcpyAsync(hostRr, &sc->rr, sizeof(double), cudaMemcpyDeviceToHost, s));
-    MFEM_CUDA(cudaMemcpyAsync(hostRr + 1, &sc->bb, sizeof(double), cudaMemcpyDeviceToHost, s));
+    k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 3, sums, nullptr);
+    k_cg_start<<<1, 1, 0, s>>>(sc, sums, rtol * rtol, maxIter);
+    MFEM_CUDA(cudaMemcpyAsync(hostSc, sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));
     MFEM_CUDA(cudaStreamSynchronize(s));
-    const double bnorm = sqrt(hostRr[1]);
-    double rel = bnorm > 0.0 ? sqrt(hostRr[0]) / bnorm : 0.0;
-    int it = 0;
-    while (it < maxIter && rel > rtol) {
-        spmv(c, vp, vq, mask, partial);                       // q = A p, partials of p . q
-        k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaRows, 1, sums);
-        k_cg_alpha<<<1, 1, 0, s>>>(sc, sums);
-        if (D == 3) k_cg_update<3><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
-        else k_cg_update<1><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
-        check_launch("k_cg_update");
-        k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 2, sums);
-        k_cg_beta<<<1, 1, 0, s>>>(sc, sums);
-        k_cg_direction<<<blocks_for((long long)n, kThreads), kThreads, 0, s>>>(sc, vz, vp, (long long)n);
-        check_launch("k_cg_direction");
-        MFEM_CUDA(cudaMemcpyAsync(hostRr, &sc->rr, sizeof(double), cudaMemcpyDeviceToHost, s));
+    // batches of iterations; every kernel of an iteration after the one that
+    // met the tolerance returns at once, so the iterate stays the converged one
+    const int *stop = &sc->stop;
+    while (!hostSc->stop) {
+        for (int k = 0; k < kCgBatch; k++) {
+            spmv(c, vp, vq, mask, partial, stop);              // q = A p, partials of p . q
+            k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaRows, 1, sums, stop);
+            k_cg_alpha<<<1, 1, 0, s>>>(sc, sums);
+            if (D == 3) k_cg_update<3><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
+            else k_cg_update<1><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
+            k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 2, sums, stop);
+            k_cg_beta<<<1, 1, 0, s>>>(sc, sums);
+            k_cg_direction<<<blocks_for((long long)n, kThreads), kThreads, 0, s>>>(sc, vz, vp, (long long)n);
+        }
+        check_launch("k_cg iteration");
+        MFEM_CUDA(cudaMemcpyAsync(hostSc, sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));
         MFEM_CUDA(cudaStreamSynchronize(s));
-        it++;
-        rel = bnorm > 0.0 ? sqrt(hostRr[0]) / bnorm : 0.0;
     }
     MFEM_CUDA(cudaMemcpyAsync(x, vx, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     MFEM_CUDA(cudaStreamSynchronize(s));
+    const double bnorm = sqrt(hostSc->bb);
+    const double rel = bnorm > 0.0 ? sqrt(hostSc->rr) / bnorm : 0.0;
+    const int it = hostSc->iter;
     if (iters) *iters = it;
     if (relres) *relres = rel;
 }
