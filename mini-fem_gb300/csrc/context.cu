@@ -247,6 +247,12 @@ long long step_async(Context &c, int op, int precision, int strategy, const doub
         c.prec.swap(P.sparePrec);
         P.cur ^= 1;
     }
+    // a slot that must grow (first use of a precision with larger values) is
+    // reallocated on the host: its last copy-out has to be finished first
+    const size_t needValues = (size_t)c.nnz * op_dim(op) * (precision == MFEM_FP32 ? 4 : 8);
+    const size_t needPrec = sizeof(double) * (size_t)c.nbNodes * op_dim(op);
+    if (P.recorded[P.cur] && (c.values.bytes < needValues || c.prec.bytes < needPrec))
+        MFEM_CUDA(cudaEventSynchronize(P.copied[P.cur]));
     if (coord) upload_coords(c, coord);
     if (coef) upload_coefficients(c, op, coef);
     assemble(c, op, precision, strategy, hostPrec != nullptr);   // waits for the slot's last copy-out
