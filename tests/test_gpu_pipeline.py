@@ -86,3 +86,26 @@ def test_synchronous_call_after_pipelined_steps(gpu):
     assert a.values().tobytes() == v.tobytes()
     with pytest.raises(Exception):
         a.wait(5)          # unknown ticket
+
+
+def test_pipelined_precision_switch(gpu):
+    """FP32, FP64, FP32 steps back to back: the slot that grows for FP64 values is
+    reallocated only after its copy-out, and every step's results stay exact."""
+    m = cube_mesh(8, seed=9, op="ela")
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    a.create_nodeToNode("sorted")
+    a.set_check_bounds(O.checkbounds(m.boundNodesCode))
+    a.set_coefficients("ela", m.coef)
+    n9 = a.nbEdges * 9
+    outs = [np.empty(n9, np.float32), np.empty(n9), np.empty(n9, np.float32)]
+    precs = [np.empty(a.nbNodes * 9) for _ in range(3)]
+    kinds = ["fp32", "fp64", "fp32"]
+    tickets = [a.step_async("ela", k, v, p) for k, v, p in zip(kinds, outs, precs)]
+    for t in tickets:
+        a.wait(t)
+    for k, v, p in zip(kinds, outs, precs):
+        a.assembly("ela", k, "gather", prec=True)
+        ref = a.values_f32() if k == "fp32" else a.values()
+        assert ref.tobytes() == v.tobytes()
+        assert a.prec().tobytes() == p.tobytes()
