@@ -210,6 +210,18 @@ def _make_slivers(coord, e2n, g, n, seed, fraction, max_aspect):
     return made
 
 
+def coefficient_set(op: str, nbElem: int, seed: int, nu_max: float = 0.35) -> np.ndarray:
+    """One more per-element coefficient set with the generator's distributions:
+    kappa ~ U[0.5, 2] (lap, [E]) or (E log-uniform in [1e9, 2e11], nu ~ U[0.2,
+    nu_max]) (ela, [E, 2])."""
+    if op == "lap":
+        return 0.5 + 1.5 * rng_uniform(seed, 3, nbElem)
+    ue = rng_uniform(seed, 4, nbElem)
+    un = rng_uniform(seed, 5, nbElem)
+    young = np.exp(np.log(1e9) + ue * (np.log(2e11) - np.log(1e9)))
+    return np.stack([young, 0.2 + un * (nu_max - 0.2)], axis=1)
+
+
 def renumber_nodes(mesh: Mesh, newOfOld: np.ndarray) -> Mesh:
     """The same mesh with node i renamed newOfOld[i] (elements keep their order)."""
     newOfOld = np.asarray(newOfOld, dtype=np.int64)
