@@ -51,3 +51,32 @@ def test_fullsize_lap_symmetry_and_row_sums(gpu, mesh):
     rs = np.add.reduceat(v, row[:-1])
     scale = np.add.reduceat(np.abs(v), row[:-1])
     assert np.max(np.abs(rs) / scale) < 1e-12
+
+
+def test_fullsize_fp32_within_tolerance_and_batch_equal(gpu, mesh):
+    """FP32 tile path at full size against the FP64 assembly (bit-identical to the
+    oracle, above): max entry error below 2e-6 of the diagonal scale, Frobenius
+    and preconditioned-operator errors below 1e-6; the batched form with one
+    coefficient set gives the same bits as the single-mesh launch."""
+    import minifem
+    from minifem import metrics
+    a = gpu(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    a.set_coefficients("ela", mesh.coef)
+    a.set_check_bounds(O.checkbounds(mesh.boundNodesCode))
+    a.assembly("ela", "fp64", "gather", prec=True)
+    v64, p64 = a.values(), a.prec()
+    a.assembly("ela", "fp32", "gather", prec=True)
+    v32, p32 = a.values_f32(), a.prec()
+    err = metrics.entry_errors(row, col, v64, v32, 9)
+    assert err["max_rel_diag_scaled"] < 2e-6, err
+    assert err["frobenius_rel"] < 1e-6, err
+    assert metrics.operator_error(row, col, v64, p64, v32, p32, 9) < 1e-6
+    b = minifem.Batch(0)
+    b.add(a, "ela", mesh.coef.reshape(1, -1, 2))
+    b.assemble("fp32", prec=True)
+    b.synchronize()
+    assert b.values(0, 0, "fp32").tobytes() == v32.tobytes()
+    assert b.prec(0, 0).tobytes() == p32.tobytes()
+    b.close()
