@@ -62,6 +62,11 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // groups instead of two.
 __device__ __forceinline__ int gslot(int l, int j) { return 4 * l + ((j + (l >> 1)) & 3); }
 
+// The gradient slots a contribution code (local element << 4 | rotated slot of
+// node j << 2 | rotated slot of node k, made by the plan) refers to.
+__device__ __forceinline__ int slot_j(unsigned u) { return (int)(u >> 2); }
+__device__ __forceinline__ int slot_k(unsigned u) { return (int)(((u >> 2) & ~3u) | (u & 3u)); }
+
 // error-free sum of two Kahan partials (value = s - c)
 __device__ __forceinline__ void kahan_merge(Kahan &a, float s2, float c2) {
     const float s = a.s + s2;
@@ -336,7 +341,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 for (int q = b + part; q < b + n; q += 4) {
                     const unsigned u = sC[q];
                     const int l = u >> 4;
-                    const float4 g = G[gslot(l, (u >> 2) & 3)];
+                    const float4 g = G[slot_j(u)];
                     acc.add(W[l].x * fmaf(g.x, g.x, fmaf(g.y, g.y, g.z * g.z)));
                 }
                 quad_combine(acc);
@@ -353,7 +358,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                     const unsigned u = sC[q];
                     const int l = u >> 4;
                     const float2 w = W[l];
-                    ela_diag_accumulate(acc, G[gslot(l, (u >> 2) & 3)], w.x, w.y);
+                    ela_diag_accumulate(acc, G[slot_j(u)], w.x, w.y);
                 }
 #pragma unroll
                 for (int m = 0; m < 6; m++) quad_combine(acc[m]);
@@ -424,7 +429,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 for (int q = b; q < b + n; q++) {
                     const unsigned u = sC[q];
                     const int l = u >> 4;
-                    const float4 gj = G[gslot(l, (u >> 2) & 3)], gk = G[gslot(l, u & 3)];
+                    const float4 gj = G[slot_j(u)], gk = G[slot_k(u)];
                     const float x = W[l].x * fmaf(gj.x, gk.x, fmaf(gj.y, gk.y, gj.z * gk.z));
                     if (q == b) { acc.s = x; acc.c = 0.f; } else acc.add(x);
                 }
@@ -436,7 +441,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 for (int q = b; q < b + n; q++) {
                     const unsigned u = sC[q];
                     const int l = u >> 4;
-                    const float4 gj = G[gslot(l, (u >> 2) & 3)], gk = G[gslot(l, u & 3)];
+                    const float4 gj = G[slot_j(u)], gk = G[slot_k(u)];
                     const float2 w = W[l];
                     ela_accumulate(acc, gj, gk, w.x, w.y, q == b);
                 }

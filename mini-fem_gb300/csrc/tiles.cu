@@ -78,6 +78,14 @@ uint32_t spread3(uint32_t v) {   // 10 bits -> every third bit
 
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+// Contribution code: local element l, and the gradient slots of its nodes j and
+// k as the tile kernel lays them out (slot of node j = (j + l / 2) mod 4, see
+// gslot), so that the kernel finds gradient j at slot index code >> 2.
+unsigned short contrib_code(int l, int j, int k) {
+    const int r = l >> 1;
+    return (unsigned short)((l << 4) | (((j + r) & 3) << 2) | ((k + r) & 3));
+}
+
 }  // namespace
 
 SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes) {
@@ -239,7 +247,7 @@ void build_tile_plan(Context &c) {
                     const int m = where(b, len, e2n[4 * (size_t)e + k]);
                     if (!keep[m]) continue;
                     contrib[T.contribBegin + base + start[m] + fill[m]++] =
-                        (unsigned short)((local[e] << 4) | (j << 2) | k);
+                        contrib_code(local[e], j, k);
                 }
             }
             bool hasDiag = false;

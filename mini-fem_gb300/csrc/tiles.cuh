@@ -19,7 +19,7 @@ struct TileDesc {
     int diagBegin, nRows, nRowsPad;          // into diagEnt: (row, meta)
     int elemBegin, nElem;                    // into elems
     int offBegin, nOff, nOffPad;             // into offEnt: (pos, transposed pos or -1, meta, 0)
-    int contribBegin, nContrib, nContribPad; // into contrib (u16: local elem << 4 | j << 2 | k)
+    int contribBegin, nContrib, nContribPad; // into contrib (u16: local elem << 4 | slot j << 2 | slot k)
     int nodeBegin, nNodes;                   // into nodes: the nodes of the tile's elements
     int mesh;                                // batch: index of the mesh the tile belongs to
 };
