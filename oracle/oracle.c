@@ -10,6 +10,9 @@
  * Compile with -O2 -ffp-contract=off so that no product/sum pair is fused: the
  * expression trees below are the reference's, operation for operation.
  */
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
@@ -177,10 +180,18 @@ static void orc_assemble_elem(const double *coord, double *values, const int *ro
     }
 }
 
+/* The loops the reference runs with OpenMP in its OMP builds -- the matrix
+ * reset (src/assembly.cc:663-666), prec_init (src/preconditioner.cc:58-85) and
+ * prec_inversion (src/preconditioner.cc:28-48) -- run in parallel here too when
+ * built with -fopenmp; the element loop stays serial, as in every reference
+ * build on this path (the REF loop, and the COLORING loop whose pragma is
+ * disabled, src/assembly.cc:362,516).  Every parallel loop writes disjoint
+ * entries, so the results do not depend on the thread count. */
 void orc_assembly(const double *coord, double *values, const int *row, const int *col,
                   const int *elemToNode, int nbElem, int nbEdges, int operatorDim,
                   int operatorID, const double *coef)
 {
+#pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)nbEdges * operatorDim; i++) values[i] = 0;
     for (long e = 0; e < nbElem; e++)
         orc_assemble_elem(coord, values, row, col, elemToNode, e, operatorDim,
@@ -218,7 +229,9 @@ void orc_assembly_ordered(const double *coord, double *values, const int *row,
 void orc_prec_init(double *prec, const double *values, const int *row, const int *col,
                    int nbNodes, int operatorDim)
 {
+#pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)nbNodes * operatorDim; i++) prec[i] = 0;
+#pragma omp parallel for schedule(static)
     for (long i = 0; i < nbNodes; i++) {
         for (int j = row[i]; j < row[i + 1]; j++) {
             if (col[j] - 1 == i) {
@@ -258,10 +271,20 @@ void orc_ela_invert_prec(int nspa, int nnt, const int *innv, const int *nnv,
     for (int k = 0; k < 9; k++) P[k] = a[k];
 }
 
+int orc_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 int orc_prec_inversion(double *prec, const int *row, const int *col,
                        const int *checkBounds, int nbNodes, int operatorID)
 {
     int nbad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nbad)
     for (int i = 0; i < nbNodes; i++) {
         if (operatorID == 0) {
             prec[i] = 1.0 / prec[i];

@@ -57,6 +57,8 @@ void orc_prec_init(double *prec, const double *values, const int *row,
 
 /* src/preconditioner.cc:25-49 prec_inversion (+ src/Fortran/elasclpr.f for ela).
  * Returns the number of blocks for which DGETRF/DGETRI reported INFO != 0. */
+/* Threads the OpenMP loops use (1 without OpenMP). */
+int orc_threads(void);
 int orc_prec_inversion(double *prec, const int *row, const int *col,
                        const int *checkBounds, int nbNodes, int operatorID);
 

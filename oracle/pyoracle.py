@@ -56,6 +56,8 @@ def port() -> C.CDLL:
         lib.orc_prec_init.argtypes = [_f64p, _f64p, _i32p, _i32p, C.c_int, C.c_int]
         lib.orc_prec_inversion.argtypes = [_f64p, _i32p, _i32p, _i32p, C.c_int, C.c_int]
         lib.orc_prec_inversion.restype = C.c_int
+        lib.orc_threads.argtypes = []
+        lib.orc_threads.restype = C.c_int
         lib.orc_dqmrd4.argtypes = [C.c_int, _i32p, C.POINTER(C.c_int), _i32p,
                                    C.POINTER(C.c_int)]
         lib.orc_e_essbcm.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _i32p, _i32p]
@@ -67,6 +69,11 @@ def port() -> C.CDLL:
         lib.orc_getrf_getri3.restype = C.c_int
         _port = lib
     return _port
+
+
+def threads() -> int:
+    """Threads of the port's OpenMP loops (matrix reset, prec_init, prec_inversion)."""
+    return int(port().orc_threads())
 
 
 def _coef_ptr(coef):
