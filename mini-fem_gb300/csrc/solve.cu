@@ -283,12 +283,12 @@ constexpr int kCgBatch = 8;
 
 }  // namespace
 
-void require_assembled(const Context &c, bool needPrec) {
+static void require_assembled(const Context &c, bool needPrec) {
     MFEM_REQUIRE(c.lastOp >= 0 && c.values.ptr, MFEM_ERR_STATE, "no assembled matrix");
     if (needPrec) MFEM_REQUIRE(c.prec.ptr && c.precIsInit, MFEM_ERR_STATE, "no preconditioner");
 }
 
-const unsigned char *solve_mask(const Context &c, int constrainedFlag) {
+static const unsigned char *solve_mask(const Context &c, int constrainedFlag) {
     return constrainedFlag && c.hasMask ? c.mask.as<unsigned char>() : nullptr;
 }
 
