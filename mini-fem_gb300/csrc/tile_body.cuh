@@ -438,11 +438,21 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 if (ent.y >= 0) values[ent.y] = v;
             } else {
                 Kahan acc[9];
-                for (int q = b; q < b + n; q++) {
+                // two contributions per pass: their shared-memory loads are in
+                // flight together (same summation order as one at a time)
+                int q = b;
+                for (; q + 1 < b + n; q += 2) {
+                    const unsigned u0 = sC[q], u1 = sC[q + 1];
+                    const float4 gj0 = G[slot_j(u0)], gk0 = G[slot_k(u0)];
+                    const float4 gj1 = G[slot_j(u1)], gk1 = G[slot_k(u1)];
+                    const float2 w0 = W[u0 >> 4], w1 = W[u1 >> 4];
+                    ela_accumulate(acc, gj0, gk0, w0.x, w0.y, q == b);
+                    ela_accumulate(acc, gj1, gk1, w1.x, w1.y, false);
+                }
+                if (q < b + n) {
                     const unsigned u = sC[q];
-                    const int l = u >> 4;
                     const float4 gj = G[slot_j(u)], gk = G[slot_k(u)];
-                    const float2 w = W[l];
+                    const float2 w = W[u >> 4];
                     ela_accumulate(acc, gj, gk, w.x, w.y, q == b);
                 }
                 float v[9];
