@@ -267,6 +267,45 @@ def test_isolated_node_and_singular_block(gpu):
         assert prec.tobytes() == ref["prec"].tobytes()
 
 
+def test_empty_mesh_is_rejected(gpu):
+    import minifem
+    a = gpu(0)
+    with pytest.raises(minifem.MfemError):
+        a.set_mesh(np.zeros((4, 3)), np.zeros((0, 4), np.int32))
+
+
+def test_degenerate_element_matches_the_reference(gpu):
+    """Elements of zero volume (two nodes made to coincide): the reference's
+    1/vol makes their gradients infinite and entries NaN or infinite; the FP64
+    gather reproduces every finite entry bit for bit and NaN where the oracle
+    has NaN (NaN payloads are the hardware's), and the FP32 path is non-finite
+    exactly where the FP64 one is."""
+    m = cube_mesh(4, seed=2, op="ela", jitter=0.0, permute=False)
+    e = m.elemToNode[10] - 1
+    coord = m.coord.copy()
+    coord[e[3]] = coord[e[0]]
+
+    class M:
+        pass
+    M.coord, M.elemToNode, M.boundNodesCode = coord, m.elemToNode, m.boundNodesCode
+    M.nbNodes, M.nbElem, M.coef = coord.shape[0], m.nbElem, m.coef
+    row, col, vals, prec = gpu_full(gpu, M, "ela", m.coef, "reference")
+    ref = O.full(M, op="ela")
+    nan = np.isnan(ref["values"])
+    assert nan.any()
+    assert np.array_equal(np.isnan(vals), nan)
+    assert vals[~nan].tobytes() == ref["values"][~nan].tobytes()
+    a = gpu(0)
+    a.set_mesh(coord, m.elemToNode)
+    a.create_nodeToNode("reference")
+    a.set_coefficients("ela", m.coef)
+    a.assembly("ela", "fp32", "gather", prec=False)
+    assert np.array_equal(np.isfinite(a.values_f32()), np.isfinite(ref["values"]))
+    fin = np.isfinite(ref["prec"])
+    assert np.array_equal(np.isfinite(prec), fin)
+    assert prec[fin].tobytes() == ref["prec"][fin].tobytes()
+
+
 def test_rcm_renumbering_is_a_permutation_and_exact(gpu):
     """RCM shrinks the bandwidth of the randomly numbered cube, and assembling the
     renumbered mesh gives the permuted matrix bit for bit (same elements, same
