@@ -67,6 +67,25 @@ __global__ void k_split_coords_t(const double *__restrict__ coord, int nbNodes,
                                 __double2float_rn(z - (double)zh), 0.f);
 }
 
+// The FP32 step's two inputs in one launch: threads [0, nbNodes) split one
+// node's coordinates, the next threads form one element's weights.
+template <int OP>
+__global__ void k_split_and_weights(const double *__restrict__ coord, int nbNodes,
+                                    float4 *__restrict__ hl, const double *__restrict__ coef,
+                                    long long nbElem, float2 *__restrict__ w) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nbNodes) {
+        const int i = (int)t;
+        const double x = coord[3 * (size_t)i], y = coord[3 * (size_t)i + 1], z = coord[3 * (size_t)i + 2];
+        const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
+        hl[2 * (size_t)i] = make_float4(xh, yh, zh, 0.f);
+        hl[2 * (size_t)i + 1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
+                                            __double2float_rn(z - (double)zh), 0.f);
+    } else if (t - nbNodes < nbElem) {
+        w[t - nbNodes] = weights32<OP>(coef, (int)(t - nbNodes));
+    }
+}
+
 uint32_t spread3(uint32_t v) {   // 10 bits -> every third bit
     v &= 0x3ff;
     v = (v | (v << 16)) & 0x030000FF;
@@ -349,8 +368,15 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     float4 *hl = (float4 *)c.scratch.reserve(sizeof(float4) * 2 * (size_t)N);
     float2 *w = (float2 *)c.tiles.w32.reserve(sizeof(float2) * (size_t)c.nbElem);
     c.timer.begin("split_coords+weights", c.stream);
-    split_coords(c, hl, c.stream);
-    weights32_all(op, c.coefOp == op ? c.coef.as<double>() : nullptr, c.nbElem, w, c.stream);
+    {
+        const double *coef = c.coefOp == op ? c.coef.as<double>() : nullptr;
+        const unsigned g = blocks_for((long long)N + c.nbElem, 256);
+        if (op == MFEM_OP_LAP)
+            k_split_and_weights<MFEM_OP_LAP><<<g, 256, 0, c.stream>>>(c.coord.as<double>(), N, hl, coef, c.nbElem, w);
+        else
+            k_split_and_weights<MFEM_OP_ELA><<<g, 256, 0, c.stream>>>(c.coord.as<double>(), N, hl, coef, c.nbElem, w);
+        check_launch("k_split_and_weights");
+    }
     c.timer.end(c.stream);
     int *st = status_ptr(c);
     MFEM_CUDA(cudaMemsetAsync(st + 4, 0, sizeof(int) * 3, c.stream));
