@@ -11,9 +11,14 @@
 //    starting from 0.0 -- the reference REF build's summation order -- and write
 //    the entry and its transpose.  Bit-exact with the reference under
 //    -fmad=false.  The diagonal kernel can also fuse prec_init + prec_inversion.
-//  * SCATTER (colour order, no atomics): one launch per colour; each element
-//    adds its 16 blocks into the values it owns within the colour.
-//  * ATOMIC: one launch, FP64 atomic adds (summation order not deterministic).
+//  * SCATTER (colour order, no atomics): the gradient records, then one launch
+//    per colour; sixteen threads per element add its 16 blocks into the values
+//    it owns within the colour.
+//  * ATOMIC: one launch, one thread per element, FP64 atomic adds (summation
+//    order not deterministic).
+#include <cstdint>
+#include <vector>
+
 #include "context.h"
 #include "elem_math.cuh"
 
@@ -180,9 +185,45 @@ k_edge_units64(const int2 *__restrict__ unitPos, int nUnits, const int *__restri
 
 // ---- element-parallel strategies (scatter within a colour / atomics) ----------
 
-template <int OP, bool COEF, bool ATOMIC>
+// Sixteen threads per element, one per ordered node pair (j, k), reading the
+// element's gradient record: block (k, j) computed on its own is bitwise the
+// transpose of block (j, k) (every product commutes), so no pair waits for
+// another.  Within a colour no two elements share a node, so the read-modify-
+// writes never collide; colours run one launch after another.
+template <int OP, bool COEF>
 __global__ void __launch_bounds__(kThreads)
-k_elem_scatter64(const int *__restrict__ elems, int count, const double *__restrict__ coord,
+k_elem_scatter64(const int *__restrict__ elems, int count, const double *__restrict__ rec,
+                 const int *__restrict__ elemPos, double *__restrict__ values) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long item = t >> 4;
+    if (item >= count) return;
+    const int jk = (int)(t & 15), j = jk >> 2, k = jk & 3;
+    const int e = elems[item];
+    const double *r = rec + (size_t)e * kRec64;
+    const int p = elemPos[(size_t)e * 16 + jk];
+    if (OP == MFEM_OP_LAP) {
+        const double v = lap_entry<!COEF>(r + 3 * j, r + 3 * k, COEF ? r[12] : 1.0);
+        values[p] = values[p] + v;
+    } else {
+        double A = 2.25, B = 1.25, mu = 1.0;
+        if (COEF) {
+            A = r[12];
+            B = r[13];
+            mu = r[14];
+        }
+        double c[9];
+        ela_block<!COEF>(r + 3 * j, r + 3 * k, A, B, mu, c);
+        double *v = values + (size_t)p * 9;
+#pragma unroll
+        for (int m = 0; m < 9; m++) v[m] = v[m] + c[m];
+    }
+}
+
+// Atomic strategy: one thread per element, gradients in registers, its ten
+// distinct blocks added with FP64 atomics (order not deterministic).
+template <int OP, bool COEF>
+__global__ void __launch_bounds__(kThreads)
+k_elem_atomic64(const int *__restrict__ elems, int count, const double *__restrict__ coord,
                  const int4 *__restrict__ e2n, const double *__restrict__ coef,
                  const int *__restrict__ elemPos, double *__restrict__ values) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -203,13 +244,8 @@ k_elem_scatter64(const int *__restrict__ elems, int count, const double *__restr
             const int pjk = pos[4 * j + k], pkj = pos[4 * k + j];
             if (OP == MFEM_OP_LAP) {
                 const double v = lap_entry<!COEF>(g + 3 * j, g + 3 * k, kappa);
-                if (ATOMIC) {
-                    atomicAdd(values + pjk, v);
-                    if (k != j) atomicAdd(values + pkj, v);
-                } else {
-                    values[pjk] = values[pjk] + v;
-                    if (k != j) values[pkj] = values[pkj] + v;
-                }
+                atomicAdd(values + pjk, v);
+                if (k != j) atomicAdd(values + pkj, v);
             } else {
                 double c[9];
                 ela_block<!COEF>(g + 3 * j, g + 3 * k, A, B, mu, c);
@@ -220,13 +256,8 @@ k_elem_scatter64(const int *__restrict__ elems, int count, const double *__restr
 #pragma unroll
                     for (int bb = 0; bb < 3; bb++) {
                         const double x = c[3 * a + bb];
-                        if (ATOMIC) {
-                            atomicAdd(vj + 3 * a + bb, x);
-                            if (k != j) atomicAdd(vk + 3 * bb + a, x);
-                        } else {
-                            vj[3 * a + bb] = vj[3 * a + bb] + x;
-                            if (k != j) vk[3 * bb + a] = vk[3 * bb + a] + x;
-                        }
+                        atomicAdd(vj + 3 * a + bb, x);
+                        if (k != j) atomicAdd(vk + 3 * bb + a, x);
                     }
             }
         }
@@ -315,26 +346,52 @@ void launch_gather(Context &c, bool fusePrec) {
 template <int OP, bool COEF>
 void launch_elementwise(Context &c, bool atomic) {
     const int dim = OP == MFEM_OP_LAP ? 1 : 9;
+    const int E = c.nbElem;
     double *vals = c.values.as<double>();
     c.timer.begin(atomic ? "atomic64" : "scatter64", c.stream);
     MFEM_CUDA(cudaMemsetAsync(vals, 0, sizeof(double) * (size_t)c.nnz * dim, c.stream));
     if (atomic) {
-        k_elem_scatter64<OP, COEF, true><<<blocks_for(c.nbElem, kThreads), kThreads, 0, c.stream>>>(
-            nullptr, c.nbElem, c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(),
+        k_elem_atomic64<OP, COEF><<<blocks_for(E, kThreads), kThreads, 0, c.stream>>>(
+            nullptr, E, c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(),
             c.elemPos.as<int>(), vals);
-        check_launch("k_elem_scatter64<atomic>");
+        check_launch("k_elem_atomic64");
         c.timer.end(c.stream);
         return;
     }
+    double *rec = (double *)c.grad.reserve(sizeof(double) * kRec64 * (size_t)E);
     const Coloring &col = c.coloring;
-    for (int k = 0; k < col.nbColors; k++) {
-        const int b = col.hOffsets[k], n = col.hOffsets[k + 1] - b;
-        if (n <= 0) continue;
-        k_elem_scatter64<OP, COEF, false><<<blocks_for(n, kThreads), kThreads, 0, c.stream>>>(
-            col.colorElems.as<int>() + b, n, c.coord.as<double>(), c.e2n.as<int4>(),
-            c.coef.as<double>(), c.elemPos.as<int>(), vals);
-        check_launch("k_elem_scatter64<colour>");
+    // the record pass and the colour loop as one CUDA graph: on small meshes a
+    // launch per colour costs more than the colour's work
+    std::vector<long long> key = {OP, COEF, (long long)(uintptr_t)rec, (long long)(uintptr_t)vals,
+                                  (long long)(uintptr_t)c.elemPos.ptr, (long long)(uintptr_t)col.colorElems.ptr,
+                                  (long long)(uintptr_t)c.coord.ptr, (long long)(uintptr_t)c.e2n.ptr,
+                                  (long long)(uintptr_t)c.coef.ptr, E};
+    key.insert(key.end(), col.hOffsets.begin(), col.hOffsets.end());
+    CachedGraph &cg = c.scatterGraph;
+    if (!cg.exec || cg.key != key) {
+        if (cg.exec) {
+            MFEM_CUDA(cudaGraphExecDestroy(cg.exec));
+            cg.exec = nullptr;
+        }
+        cudaGraph_t graph;
+        MFEM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        k_grad64<OP, COEF><<<blocks_for(E, kThreads), kThreads, 0, c.stream>>>(
+            c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(), E, rec);
+        for (int k = 0; k < col.nbColors; k++) {
+            const int b = col.hOffsets[k], n = col.hOffsets[k + 1] - b;
+            if (n <= 0) continue;
+            k_elem_scatter64<OP, COEF><<<blocks_for(16LL * n, kThreads), kThreads, 0, c.stream>>>(
+                col.colorElems.as<int>() + b, n, rec, c.elemPos.as<int>(), vals);
+        }
+        const cudaError_t launchErr = cudaGetLastError();
+        MFEM_CUDA(cudaStreamEndCapture(c.stream, &graph));
+        MFEM_CUDA(launchErr);
+        const cudaError_t instErr = cudaGraphInstantiate(&cg.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        MFEM_CUDA(instErr);
+        cg.key.swap(key);
     }
+    MFEM_CUDA(cudaGraphLaunch(cg.exec, c.stream));
     c.timer.end(c.stream);
 }
 

@@ -79,6 +79,19 @@ struct Pipeline {
     ~Pipeline();
 };
 
+// An instantiated CUDA graph with the arguments it was captured with; a
+// launch whose arguments differ re-captures it.
+struct CachedGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long long> key;
+    CachedGraph() = default;
+    CachedGraph(const CachedGraph &) = delete;
+    CachedGraph &operator=(const CachedGraph &) = delete;
+    ~CachedGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
 struct Context {
     int device = 0;
     KernelTimer timer;
@@ -135,6 +148,7 @@ struct Context {
     DevBuf solver;                    // CG work vectors (solve.cu)
     DevBuf scratch, scratch2, scanTmp;
     DevBuf status;                    // int[8] device-side error flags
+    CachedGraph scatterGraph;         // the colour-ordered scatter (asm64.cu)
 
     // last member: destroyed first, so that its copies finish before the
     // buffers they read are freed
