@@ -183,6 +183,24 @@ k_edge_units64(const int2 *__restrict__ unitPos, int nUnits, const int *__restri
     }
 }
 
+// The weight fields of the gradient records (A, B, mu or kappa) for another
+// coefficient set on the same mesh; the gradients stay.
+template <int OP>
+__global__ void __launch_bounds__(kThreads)
+k_weights64(const double *__restrict__ coef, int nbElem, double *__restrict__ rec) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nbElem) return;
+    double2 *out = reinterpret_cast<double2 *>(rec + (size_t)e * kRec64);
+    if (OP == MFEM_OP_LAP) {
+        out[6] = make_double2(coef[e], 0.0);
+    } else {
+        double A, B, mu;
+        lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
+        out[6] = make_double2(A, B);
+        out[7] = make_double2(mu, 0.0);
+    }
+}
+
 // ---- element-parallel strategies (scatter within a colour / atomics) ----------
 
 // Sixteen threads per element, one per ordered node pair (j, k), reading the
@@ -472,7 +490,8 @@ void gather_fp64_into(const Context &c, int op, const double *coord, const doubl
 // preconditioner when prec != NULL (batched assembly; same kernels and results
 // as assemble_fp64 with the gather strategy).
 void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec, double *values,
-                      double *prec, const unsigned char *mask, int *singular, cudaStream_t s) {
+                      double *prec, const unsigned char *mask, int *singular, cudaStream_t s,
+                      bool gradientsReady) {
     const GatherPlan &g = c.gather;
     const int E = c.nbElem, N = c.nbNodes;
     const int *dp = c.diagPos.as<int>(), *st = g.unitStart.as<int>();
@@ -481,7 +500,14 @@ void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec,
     const int4 *e2n = c.e2n.as<int4>();
     const double *coord = c.coord.as<double>();
     auto run = [&](auto grad, auto diag, auto diagp, auto edge) {
-        grad<<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
+        // the records' gradients depend on the mesh only: after the first set
+        // of a mesh only the weights are rewritten (none at all for constants)
+        if (!gradientsReady) {
+            grad<<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
+        } else if (coef) {
+            if (op == MFEM_OP_LAP) k_weights64<MFEM_OP_LAP><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coef, E, rec);
+            else k_weights64<MFEM_OP_ELA><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coef, E, rec);
+        }
         if (prec)
             diagp<<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, prec, mask, singular);
         else

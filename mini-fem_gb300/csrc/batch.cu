@@ -7,8 +7,9 @@
 // counter; each item computes the
 // tile's gradients once and its entries and preconditioner blocks for every
 // coefficient set of its mesh.
-// FP64: the graph holds, per mesh and set, the three bit-exact gather launches
-// (records, diagonal units + preconditioner, off-diagonal units).
+// FP64: the graph holds, per mesh and set, the bit-exact gather launches:
+// gradient records (for the first set of a mesh; later sets rewrite only the
+// records' weights), diagonal units + preconditioner, off-diagonal units.
 // Results equal the single-mesh entry points' bit for bit (same plans, same
 // arithmetic).  No counterpart in the reference, which assembles one mesh per
 // rank (src/FEM.cc:177-257).
@@ -31,7 +32,8 @@ struct BatchMesh {
 };
 
 void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec, double *values,
-                      double *prec, const unsigned char *mask, int *singular, cudaStream_t s);
+                      double *prec, const unsigned char *mask, int *singular, cudaStream_t s,
+                      bool gradientsReady);
 
 }  // namespace mfem
 
@@ -242,7 +244,7 @@ void record64(mfem_batch &b, bool withPrec) {
             double *prec = withPrec ? b.prec.as<double>() + it->precOff + (size_t)s * c.nbNodes * dim
                                     : nullptr;
             gather_fp64_sets(c, it->op, coef, b.recs.as<double>(), vals, prec,
-                             c.hasMask ? c.mask.as<unsigned char>() : nullptr, cnt, b.stream);
+                             c.hasMask ? c.mask.as<unsigned char>() : nullptr, cnt, b.stream, s > 0);
         }
     }
 }
