@@ -290,8 +290,11 @@ void assemble_fp32(Context &c, int op, int strategy, bool fusePrec) {
     MFEM_REQUIRE(strategy == MFEM_GATHER, MFEM_ERR_INVALID_ARG,
                  "FP32 assembly offers the gather strategy");
     if (c.fp32Kernel == 1) {
-        assemble_tiles32(c, op, fusePrec);
-        return;
+        build_tile_plan(c);
+        if (!c.tiles.unfit) {
+            assemble_tiles32(c, op, fusePrec);
+            return;
+        }
     }
     const bool coef = c.coefOp == op;
     const int dim = op == MFEM_OP_LAP ? 1 : 9;

@@ -109,6 +109,8 @@ void prepare(mfem_batch &b) {
         auto *it = b.items[m];
         Context &c = it->ctx->c;
         build_tile_plan(c);
+        MFEM_REQUIRE(!c.tiles.unfit, MFEM_ERR_CAPACITY,
+                     "batch: a mesh does not fit the tiles (a node touching more elements than a tile holds)");
         build_gather_plan(c);
         it->valOff = b.totalVal;
         it->precOff = b.totalPrec;

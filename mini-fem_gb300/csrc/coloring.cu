@@ -167,7 +167,7 @@ void build_coloring(Context &c, unsigned long long seed) {
     col.hOffsets.resize(nColors + 1);
     exclusive_scan_i32(hist, hist, (long long)nColors * nTiles, tmp, c.stream);
     int *elems = (int *)col.colorElems.reserve(sizeof(int) * (size_t)E);
-    int *perm = (int *)c.scratch2.reserve(sizeof(int) * (size_t)E);
+    int *perm = (int *)col.perm.reserve(sizeof(int) * (size_t)E);
     k_color_tile_place<<<nTiles, 32, 0, c.stream>>>(color, E, nTiles, hist, elems, perm);
     check_launch("k_color_tile_place");
     col.nbColors = nColors;

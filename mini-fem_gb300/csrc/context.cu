@@ -419,7 +419,7 @@ int mfem_coloring_creation(mfem_context *ctx, unsigned long long seed, int *colo
         const int nc = c.coloring.nbColors;
         if (nbColors) *nbColors = nc;
         if (colorPerm)
-            MFEM_CUDA(cudaMemcpyAsync(colorPerm, c.scratch2.as<int>(), sizeof(int) * (size_t)c.nbElem,
+            MFEM_CUDA(cudaMemcpyAsync(colorPerm, c.coloring.perm.as<int>(), sizeof(int) * (size_t)c.nbElem,
                                       cudaMemcpyDeviceToHost, c.stream));
         MFEM_CUDA(cudaStreamSynchronize(c.stream));
         if (colorIndex) {

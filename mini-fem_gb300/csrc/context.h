@@ -32,6 +32,7 @@ struct GatherPlan {
 // most maxRows rows touching at most maxElem elements.
 struct TilePlan {
     bool built = false;
+    bool unfit = false;         // built, but the mesh does not fit the tiles
     int maxRows = 48, maxElem = 512;
     int nTiles = 0;
     long long nTileElems = 0;   // sum over tiles of their element counts
@@ -48,6 +49,7 @@ struct Coloring {
     std::vector<int> hOffsets;   // nbColors + 1, into colorElems
     DevBuf color;                // int [E]
     DevBuf colorElems;           // int [E] elements sorted by colour (stable)
+    DevBuf perm;                 // int [E] new position of each element (colorPerm)
 };
 
 // Optional per-kernel CUDA-event timing (mfem_profile): each named launch

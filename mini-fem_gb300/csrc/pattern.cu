@@ -17,6 +17,9 @@
 //   4. gather plan: one thread per row walks its incident elements in ascending
 //      order and appends (e, j, k) to the unit of entry (r, node_k) for every
 //      node_k >= r, so every unit list comes out ascending by construction.
+#include <algorithm>
+#include <vector>
+
 #include "context.h"
 
 namespace mfem {
@@ -26,7 +29,7 @@ namespace {
 constexpr int kMaxRow = 128;   // longest row (distinct neighbours incl. self)
 constexpr int kThreads = 256;
 
-enum StatusBits { kRowOverflow = 1, kMissingEntry = 2, kBadIndex = 4 };
+enum StatusBits { kMissingEntry = 2, kBadIndex = 4 };
 
 __global__ void k_to_zero_based(const int *__restrict__ in, int *__restrict__ out,
                                 long long n, int nbNodes, int *status) {
@@ -102,16 +105,21 @@ __device__ int row_neighbours(int r, const int *__restrict__ ptr,
     return cnt;
 }
 
+// Rows longer than kMaxRow are listed in longRows (count in *nLong) and sized
+// and written by k_long_row, one CTA each.
 template <int ORDER>
 __global__ void k_row_count(const int *__restrict__ ptr, const int *__restrict__ nodeElem,
                             const int *__restrict__ e2n, int nbNodes, int *rowLen,
-                            int *status) {
+                            int *longRows, int *nLong) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nbNodes) return;
     int uniq[kMaxRow];
     bool overflow = false;
     int cnt = row_neighbours<ORDER>(r, ptr, nodeElem, e2n, uniq, overflow);
-    if (overflow) atomicOr(status, kRowOverflow);
+    if (overflow) {
+        longRows[atomicAdd(nLong, 1)] = r;
+        cnt = 0;
+    }
     rowLen[r] = cnt;
 }
 
@@ -124,6 +132,7 @@ __global__ void k_row_write(const int *__restrict__ ptr, const int *__restrict__
     int uniq[kMaxRow];
     bool overflow = false;
     int cnt = row_neighbours<ORDER>(r, ptr, nodeElem, e2n, uniq, overflow);
+    if (overflow) return;   // a long row: k_long_row writes it
     int base = rowPtr[r];
     int dp = -1;
     for (int m = 0; m < cnt; m++) {
@@ -131,6 +140,82 @@ __global__ void k_row_write(const int *__restrict__ ptr, const int *__restrict__
         if (uniq[m] == r) dp = base + m;
     }
     diagPos[r] = dp;
+}
+
+// One CTA per long row: the row's 4 x (incident elements) candidate columns,
+// with their candidate index (incident element order, then node slot), are
+// sorted in shared memory (bitonic, P a power of two); the first of each run of
+// equal columns is a distinct neighbour, and its candidate index is its first
+// occurrence.  WRITE = false: the row length; true: the columns in sorted or
+// first-occurrence order, and the diagonal position.
+__device__ __forceinline__ bool pair_less(int2 a, int2 b) {
+    return a.x != b.x ? a.x < b.x : a.y < b.y;
+}
+
+template <int ORDER, bool WRITE>
+__global__ void k_long_row(const int *__restrict__ longRows, const int *__restrict__ ptr,
+                           const int *__restrict__ nodeElem, const int *__restrict__ e2n, int P,
+                           int *rowLen, const int *__restrict__ rowPtr, int *col, int *diagPos) {
+    extern __shared__ int2 buf[];                       // P pairs, then P first-occurrence flags
+    int *first = reinterpret_cast<int *>(buf + P);
+    __shared__ int part[kThreads + 1];
+    const int r = longRows[blockIdx.x];
+    const int b = ptr[r], M = 4 * (ptr[r + 1] - b);    // M <= P (sized on the host)
+    const int tid = threadIdx.x;
+    for (int i = tid; i < P; i += kThreads) {
+        buf[i] = i < M ? make_int2(e2n[4 * (nodeElem[b + (i >> 2)] >> 2) + (i & 3)], i)
+                       : make_int2(0x7fffffff, 0x7fffffff);
+        first[i] = 0;
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < P; i += kThreads) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const int2 a = buf[i], c = buf[ixj];
+                    if (pair_less(c, a) == ((i & k) == 0)) {
+                        buf[i] = c;
+                        buf[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    // distinct columns: the first of each run; ORDER_SORTED keeps the sorted
+    // position, ORDER_REFERENCE the position of the first occurrence
+    for (int i = tid; i < M; i += kThreads) {
+        const bool head = i == 0 || buf[i].x != buf[i - 1].x;
+        if (head) first[ORDER == MFEM_ORDER_SORTED ? i : buf[i].y] = 1;
+    }
+    __syncthreads();
+    const int chunk = (P + kThreads - 1) / kThreads, lo = min(P, tid * chunk), hi = min(P, lo + chunk);
+    int cnt = 0;
+    for (int i = lo; i < hi; i++) cnt += first[i];
+    part[tid] = cnt;
+    __syncthreads();
+    if (tid == 0) {
+        int run = 0;
+        for (int t = 0; t < kThreads; t++) {
+            const int v = part[t];
+            part[t] = run;
+            run += v;
+        }
+        part[kThreads] = run;
+        if (!WRITE) rowLen[r] = run;
+    }
+    __syncthreads();
+    if (!WRITE) return;
+    int pos = rowPtr[r] + part[tid];
+    for (int i = lo; i < hi; i++) {
+        if (!first[i]) continue;
+        // sorted: the column at sorted position i; first occurrence: candidate i
+        const int c = ORDER == MFEM_ORDER_SORTED ? buf[i].x
+                                                 : e2n[4 * (nodeElem[b + (i >> 2)] >> 2) + (i & 3)];
+        col[pos] = c;
+        if (c == r) diagPos[r] = pos;
+        pos++;
+    }
 }
 
 __device__ __forceinline__ int find_pos(const int *__restrict__ col, int b, int e, int c,
@@ -269,8 +354,6 @@ void check_status(Context &c, const char *what) {
     read_status(c, &st, 1);
     if (st & kBadIndex)
         throw Error(MFEM_ERR_INVALID_ARG, std::string(what) + ": elemToNode index out of range");
-    if (st & kRowOverflow)
-        throw Error(MFEM_ERR_PATTERN, std::string(what) + ": a row has more than 128 entries");
     if (st & kMissingEntry)
         throw Error(MFEM_ERR_PATTERN, std::string(what) + ": pattern misses an element pair");
 }
@@ -307,11 +390,40 @@ void build_pattern(Context &c, int order) {
     int *rowPtr = (int *)c.rowPtr.reserve(sizeof(int) * (N + 1));
     int *tmp = (int *)c.scanTmp.reserve(sizeof(int) * scan_tmp_elems(N + 1));
     const int *ptr = c.nodeElemPtr.as<int>(), *ne = c.nodeElem.as<int>(), *e2n = c.e2n.as<int>();
+    int *longRows = (int *)c.scratch2.reserve(sizeof(int) * ((size_t)N + 1));
+    int *nLongDev = longRows + N;
+    MFEM_CUDA(cudaMemsetAsync(nLongDev, 0, sizeof(int), c.stream));
     if (order == MFEM_ORDER_SORTED)
-        k_row_count<MFEM_ORDER_SORTED><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, st);
+        k_row_count<MFEM_ORDER_SORTED><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, longRows, nLongDev);
     else
-        k_row_count<MFEM_ORDER_REFERENCE><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, st);
+        k_row_count<MFEM_ORDER_REFERENCE><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, longRows, nLongDev);
     check_launch("k_row_count");
+    // rows longer than the per-thread list: one CTA each, candidates sorted in
+    // shared memory (P = the next power of two of 4 x the largest valence)
+    int nLong = 0, P = 0;
+    MFEM_CUDA(cudaMemcpyAsync(&nLong, nLongDev, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    MFEM_CUDA(cudaStreamSynchronize(c.stream));
+    if (nLong > 0) {
+        std::vector<int> rows(nLong), hptr(N + 1);
+        MFEM_CUDA(cudaMemcpyAsync(rows.data(), longRows, sizeof(int) * nLong, cudaMemcpyDeviceToHost, c.stream));
+        MFEM_CUDA(cudaMemcpyAsync(hptr.data(), ptr, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost, c.stream));
+        MFEM_CUDA(cudaStreamSynchronize(c.stream));
+        int maxM = 0;
+        for (int r : rows) maxM = std::max(maxM, 4 * (hptr[r + 1] - hptr[r]));
+        P = 1;
+        while (P < maxM) P <<= 1;
+        MFEM_REQUIRE((size_t)P * 12 <= 200 * 1024, MFEM_ERR_CAPACITY,
+                     "create_nodeToNode: a node has more than 4096 incident elements");
+        const size_t smem = (size_t)P * 12;
+        if (order == MFEM_ORDER_SORTED) {
+            MFEM_CUDA(cudaFuncSetAttribute(k_long_row<MFEM_ORDER_SORTED, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_long_row<MFEM_ORDER_SORTED, false><<<nLong, kThreads, smem, c.stream>>>(longRows, ptr, ne, e2n, P, rowPtr, nullptr, nullptr, nullptr);
+        } else {
+            MFEM_CUDA(cudaFuncSetAttribute(k_long_row<MFEM_ORDER_REFERENCE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_long_row<MFEM_ORDER_REFERENCE, false><<<nLong, kThreads, smem, c.stream>>>(longRows, ptr, ne, e2n, P, rowPtr, nullptr, nullptr, nullptr);
+        }
+        check_launch("k_long_row");
+    }
     exclusive_scan_i32(rowPtr, rowPtr, N, tmp, c.stream);
     int nnz = 0;
     MFEM_CUDA(cudaMemcpyAsync(&nnz, rowPtr + N, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -324,6 +436,17 @@ void build_pattern(Context &c, int order) {
     else
         k_row_write<MFEM_ORDER_REFERENCE><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, e2n, N, rowPtr, col, diag);
     check_launch("k_row_write");
+    if (nLong > 0) {
+        const size_t smem = (size_t)P * 12;
+        if (order == MFEM_ORDER_SORTED) {
+            MFEM_CUDA(cudaFuncSetAttribute(k_long_row<MFEM_ORDER_SORTED, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_long_row<MFEM_ORDER_SORTED, true><<<nLong, kThreads, smem, c.stream>>>(longRows, ptr, ne, e2n, P, nullptr, rowPtr, col, diag);
+        } else {
+            MFEM_CUDA(cudaFuncSetAttribute(k_long_row<MFEM_ORDER_REFERENCE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_long_row<MFEM_ORDER_REFERENCE, true><<<nLong, kThreads, smem, c.stream>>>(longRows, ptr, ne, e2n, P, nullptr, rowPtr, col, diag);
+        }
+        check_launch("k_long_row");
+    }
     c.nnz = nnz;
     c.order = order;
     c.hasPattern = true;

@@ -120,9 +120,31 @@ SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRow
 }
 
 // Host-side plan construction (once per mesh and pattern).
+namespace {
+void build_tile_plan_impl(Context &c);
+}
+
+// A mesh the tiles cannot hold (a node touching more elements than a tile,
+// an entry with more than 255 contributions, a layout beyond shared memory) is
+// marked unfit: the FP32 path then uses the record kernel, which has no such
+// limit.
 void build_tile_plan(Context &c) {
     TilePlan &tp = c.tiles;
     if (tp.built) return;
+    tp.unfit = false;
+    try {
+        build_tile_plan_impl(c);
+    } catch (const Error &e) {
+        if (e.code != MFEM_ERR_CAPACITY) throw;
+        tp.unfit = true;
+        tp.built = true;
+    }
+}
+
+namespace {
+
+void build_tile_plan_impl(Context &c) {
+    TilePlan &tp = c.tiles;
     build_incidence(c);
     const int N = c.nbNodes, E = c.nbElem, nnz = c.nnz;
     std::vector<double> coord((size_t)N * 3);
@@ -335,6 +357,8 @@ void build_tile_plan(Context &c) {
     tp.built = true;
 }
 
+}  // namespace
+
 TilePlanView plan_view(const TilePlan &tp) {
     TilePlanView P;
     P.desc = tp.desc.as<TileDesc>();
@@ -428,6 +452,8 @@ extern "C" int mfem_tile_info(mfem_context *ctx, int *nbTiles, long long *nbTile
         MFEM_REQUIRE(ctx->c.hasPattern, MFEM_ERR_STATE, "no CSR pattern");
         mfem::build_tile_plan(ctx->c);
         const mfem::TilePlan &tp = ctx->c.tiles;
+        MFEM_REQUIRE(!tp.unfit, MFEM_ERR_CAPACITY,
+                     "tile plan: the mesh does not fit the tiles (the FP32 path uses the record kernel)");
         if (nbTiles) *nbTiles = tp.nTiles;
         if (nbTileElems) *nbTileElems = tp.nTileElems;
         if (nbUnits) *nbUnits = tp.nUnits;

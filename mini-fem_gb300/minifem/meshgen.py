@@ -210,6 +210,64 @@ def _make_slivers(coord, e2n, g, n, seed, fraction, max_aspect):
     return made
 
 
+def _icosphere(subdivisions: int):
+    """Unit icosphere: vertices [V, 3] and outward-oriented triangles [F, 3]
+    (each subdivision splits a triangle into four at its edge midpoints)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+         (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9),
+             (5, 11, 4), (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2),
+             (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+             (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                mid[key] = len(verts) - 1
+            return mid[key]
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts), np.array(faces, dtype=np.int64)
+
+
+def fan_mesh(subdivisions: int, seed: int = 0, *, op: str = "ela",
+             permute: bool = True) -> Mesh:
+    """A ball of tetrahedra that all share its centre node: one tetrahedron per
+    triangle of an icosphere (20 * 4**subdivisions of them), so the centre's CSR
+    row holds every node of the mesh.  A worst case for row lengths and for
+    elements per node (1280 at 3 subdivisions), where the cube has at most 24.
+    Surface nodes in the lower half (z < 0) are fixed in all directions."""
+    sv, tri = _icosphere(subdivisions)
+    N = len(sv) + 1
+    coord = np.vstack([np.zeros((1, 3)), sv])
+    e2n = np.concatenate([np.zeros((len(tri), 1), np.int64), tri + 1], axis=1)
+    code = np.zeros(N, dtype=np.int32)
+    code[1:][sv[:, 2] < 0.0] = JL_OUT
+    if permute:
+        keys = rng_u64(seed, 2, N)
+        order = np.argsort(keys, kind="stable")
+        new_of_old = np.empty(N, dtype=np.int64)
+        new_of_old[order] = np.arange(N, dtype=np.int64)
+        coord, code, e2n = coord[order], code[order], new_of_old[e2n]
+        e2n = e2n[np.argsort(rng_u64(seed, 7, len(e2n)), kind="stable")]
+    F = len(tri)
+    nnz = N + 2 * (3 * F // 2 + (N - 1))      # diagonal + both directions of every edge
+    return Mesh(coord=np.ascontiguousarray(coord),
+                elemToNode=np.ascontiguousarray((e2n + 1).astype(np.int32)),
+                boundNodesCode=code, nbEdges=nnz,
+                coef=coefficient_set(op, F, seed), op=op,
+                meta={"subdivisions": subdivisions, "seed": seed, "centre_elements": F})
+
+
 def coefficient_set(op: str, nbElem: int, seed: int, nu_max: float = 0.35) -> np.ndarray:
     """One more per-element coefficient set with the generator's distributions:
     kappa ~ U[0.5, 2] (lap, [E]) or (E log-uniform in [1e9, 2e11], nu ~ U[0.2,

@@ -1,7 +1,8 @@
 import numpy as np
 import pytest
 
-from minifem.meshgen import (cube_mesh, cube_sizes, read_reference_input,
+import pyoracle as O
+from minifem.meshgen import (cube_mesh, cube_sizes, fan_mesh, read_reference_input,
                              write_reference_input)
 
 
@@ -64,3 +65,19 @@ def test_truncated_file_is_rejected(tmp_path):
     p.write_bytes(data[: len(data) // 2])
     with pytest.raises(ValueError):
         read_reference_input(str(p))
+
+
+@pytest.mark.parametrize("subdivisions", [1, 2, 3])
+def test_fan_mesh_centre_row_holds_every_node(subdivisions):
+    """Every tetrahedron of the fan mesh touches the centre node: its row holds
+    all nodes, the element volumes are positive in the reference's orientation,
+    and the stated CSR size is the pattern's."""
+    m = fan_mesh(subdivisions, seed=3)
+    F = 20 * 4 ** subdivisions
+    assert m.nbElem == F and m.nbNodes == 10 * 4 ** subdivisions + 3
+    row, col = O.pattern(m.elemToNode, m.nbNodes)
+    assert int(row[-1]) == m.nbEdges
+    assert np.diff(row).max() == m.nbNodes
+    X = m.coord[m.elemToNode - 1]
+    a, b, c = X[:, 0] - X[:, 3], X[:, 2] - X[:, 3], X[:, 1] - X[:, 3]
+    assert np.einsum("ij,ij->i", a, np.cross(b, c)).min() > 0.0
