@@ -267,6 +267,14 @@ int mfem_batch_get_prec(mfem_batch *batch, int item, int set, double *prec);
 int mfem_batch_info(mfem_batch *batch, int *nbItems, long long *nbElemTotal,
                     long long *nbAssemblies, int *nbWork, int *grid);
 
+/* ---- self-test ------------------------------------------------------------- */
+/* The FP64 kernels form part of their products on the integer pipes (a
+ * correctly rounded multiplication with the FP64 unit's bits).  Compares that
+ * multiplication with the FP64 unit on n seeded operand pairs on ctx's device:
+ * *fastPath = pairs it handled, *mismatches = pairs whose bits differ (0). */
+int mfem_selftest_dmul(mfem_context *ctx, long long n, unsigned long long seed,
+                       unsigned long long *fastPath, unsigned long long *mismatches);
+
 /* ---- reference-shaped single calls (host buffers in and out) ---------------- */
 /* Same arguments and meaning as the reference operators; each call uploads what
  * it reads and downloads what it writes.  nodeToNodeRow / nodeToNodeColumn must

@@ -28,6 +28,54 @@ namespace {
 
 constexpr int kThreads = 128;
 
+// Multiply splits (elem_math.cuh) of the FP64 kernels, chosen by timing the
+// 5.8M-tet elasticity cube: the gradient kernel sends its cross products and
+// 1/vol scalings to the integer pipes, the diagonal units their gradient products
+// and diagonal weightings, the off-diagonal units their gradient products and B
+// weightings (1009 -> 1626 M elem/s for the FP64 step, with the locality order).
+constexpr int kSplitGrad = kIntCross | kIntScale;
+constexpr int kSplitDiag = kIntGrad | kIntDiagW;
+constexpr int kSplitEdge = kIntGrad | kIntOffW;
+
+// Chunk j of a gradient record: g_j into g, the weight of its spare slot
+// returned.  Records are 32-byte aligned and read-only in the kernels that read
+// them (written by an earlier launch).
+__device__ __forceinline__ double ld_chunk(const double *R, unsigned j, double g[3]) {
+    double w;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(g[0]), "=d"(g[1]), "=d"(g[2]), "=d"(w)
+        : "l"(R + 4 * j));
+    return w;
+}
+
+// (A, B, mu) of an ela record given the chunks j and k already loaded: A is in
+// chunks 0 and 3, B in 1, mu in 2; the others come from their slots.
+__device__ __forceinline__ void ela_weights(const double *R, unsigned j, double wj, unsigned k,
+                                            double wk, double &A, double &B, double &mu) {
+    if (j == 0 || j == 3) A = wj;
+    else if (k == 0 || k == 3) A = wk;
+    else A = __ldg(R + 3);
+    if (j == 1) B = wj;
+    else if (k == 1) B = wk;
+    else B = __ldg(R + 7);
+    if (j == 2) mu = wj;
+    else if (k == 2) mu = wk;
+    else mu = __ldg(R + 11);
+}
+
+__device__ __forceinline__ void store_record(double *rec, int e, const double g[12], double w0,
+                                             double w1, double w2, double w3) {
+    double2 *out = reinterpret_cast<double2 *>(rec + (size_t)e * kRec64);
+    out[0] = make_double2(g[0], g[1]);
+    out[1] = make_double2(g[2], w0);
+    out[2] = make_double2(g[3], g[4]);
+    out[3] = make_double2(g[5], w1);
+    out[4] = make_double2(g[6], g[7]);
+    out[5] = make_double2(g[8], w2);
+    out[6] = make_double2(g[9], g[10]);
+    out[7] = make_double2(g[11], w3);
+}
+
 __device__ __forceinline__ double fix_zero(double x) {
     // 0.0 + x: identical to x except that -0.0 becomes +0.0 (integer pipe)
     const long long b = __double_as_longlong(x);
@@ -41,38 +89,31 @@ k_grad64(const double *__restrict__ coord, const int4 *__restrict__ e2n,
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nbElem) return;
     double g[12];
-    elem_gradients(coord, e2n[e], g);
-    double2 *out = reinterpret_cast<double2 *>(rec + (size_t)e * kRec64);
-#pragma unroll
-    for (int i = 0; i < 6; i++) out[i] = make_double2(g[2 * i], g[2 * i + 1]);
-    if (COEF) {
-        if (OP == MFEM_OP_LAP) {
-            out[6] = make_double2(coef[e], 0.0);
-        } else {
-            double A, B, mu;
-            lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
-            out[6] = make_double2(A, B);
-            out[7] = make_double2(mu, 0.0);
-        }
+    elem_gradients<kSplitGrad>(coord, e2n[e], g);
+    if (!COEF) {
+        store_record(rec, e, g, 0.0, 0.0, 0.0, 0.0);
+    } else if (OP == MFEM_OP_LAP) {
+        const double kappa = coef[e];
+        store_record(rec, e, g, kappa, kappa, kappa, kappa);
+    } else {
+        double A, B, mu;
+        lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
+        store_record(rec, e, g, A, B, mu, A);
     }
-}
-
-__device__ __forceinline__ void load3(const double *p, double *g) {
-    g[0] = p[0];
-    g[1] = p[1];
-    g[2] = p[2];
 }
 
 // Diagonal units: entry (r, r) = sum over incident elements (ascending) of
 // block (j, j).  Optionally fused with prec_init + prec_inversion.
 template <int OP, bool COEF, bool PREC>
 __global__ void __launch_bounds__(kThreads)
-k_diag_units64(const int *__restrict__ diagPos, const int *__restrict__ start,
-               const unsigned *__restrict__ contrib, const double *__restrict__ rec,
-               int nbNodes, double *__restrict__ values, double *__restrict__ prec,
-               const unsigned char *__restrict__ mask, int *singular) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nbNodes) return;
+k_diag_units64(const int *__restrict__ diagNode, const int *__restrict__ diagPos,
+               const int *__restrict__ start, const unsigned *__restrict__ contrib,
+               const double *__restrict__ rec, int nbNodes, double *__restrict__ values,
+               double *__restrict__ prec, const unsigned char *__restrict__ mask,
+               int *singular) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nbNodes) return;
+    const int r = diagNode[t];
     const int p = diagPos[r];
     if (OP == MFEM_OP_LAP) {
         double acc = 0.0;
@@ -82,8 +123,8 @@ k_diag_units64(const int *__restrict__ diagPos, const int *__restrict__ start,
                 const unsigned u = contrib[q];
                 const double *R = rec + (size_t)(u >> 4) * kRec64;
                 double g[3];
-                load3(R + 3 * ((u >> 2) & 3), g);
-                const double v = lap_entry<!COEF>(g, g, COEF ? R[12] : 1.0);
+                const double kappa = ld_chunk(R, (u >> 2) & 3, g);
+                const double v = lap_entry<!COEF, kSplitDiag>(g, g, kappa);
                 acc = (q == b) ? fix_zero(v) : acc + v;
             }
             values[p] = acc;
@@ -97,11 +138,12 @@ k_diag_units64(const int *__restrict__ diagPos, const int *__restrict__ start,
         for (int q = b; q < en; q++) {
             const unsigned u = contrib[q];
             const double *R = rec + (size_t)(u >> 4) * kRec64;
+            const unsigned j = (u >> 2) & 3;
             double g[3], d[6];
-            load3(R + 3 * ((u >> 2) & 3), g);
+            const double wj = ld_chunk(R, j, g);
             double A = 0.0, B = 0.0, mu = 0.0;
-            if (COEF) { A = R[12]; B = R[13]; mu = R[14]; }
-            ela_diag_block<!COEF>(g, A, B, mu, d);
+            if (COEF) ela_weights(R, j, wj, j, wj, A, B, mu);
+            ela_diag_block<!COEF, kSplitDiag>(g, A, B, mu, d);
             if (q == b) {
 #pragma unroll
                 for (int m = 0; m < 6; m++) acc[m] = fix_zero(d[m]);
@@ -143,9 +185,9 @@ k_edge_units64(const int2 *__restrict__ unitPos, int nUnits, const int *__restri
             const unsigned u = contrib[q];
             const double *R = rec + (size_t)(u >> 4) * kRec64;
             double gj[3], gk[3];
-            load3(R + 3 * ((u >> 2) & 3), gj);
-            load3(R + 3 * (u & 3), gk);
-            const double v = lap_entry<!COEF>(gj, gk, COEF ? R[12] : 1.0);
+            const double kappa = ld_chunk(R, (u >> 2) & 3, gj);
+            ld_chunk(R, u & 3, gk);
+            const double v = lap_entry<!COEF, kSplitEdge>(gj, gk, kappa);
             acc = (q == b) ? fix_zero(v) : acc + v;
         }
         values[pp.x] = acc;
@@ -157,12 +199,12 @@ k_edge_units64(const int2 *__restrict__ unitPos, int nUnits, const int *__restri
     for (int q = b; q < en; q++) {
         const unsigned u = contrib[q];
         const double *R = rec + (size_t)(u >> 4) * kRec64;
+        const unsigned j = (u >> 2) & 3, k = u & 3;
         double gj[3], gk[3], c[9];
-        load3(R + 3 * ((u >> 2) & 3), gj);
-        load3(R + 3 * (u & 3), gk);
+        const double wj = ld_chunk(R, j, gj), wk = ld_chunk(R, k, gk);
         double A = 0.0, B = 0.0, mu = 0.0;
-        if (COEF) { A = R[12]; B = R[13]; mu = R[14]; }
-        ela_block<!COEF>(gj, gk, A, B, mu, c);
+        if (COEF) ela_weights(R, j, wj, k, wk, A, B, mu);
+        ela_block<!COEF, kSplitEdge>(gj, gk, A, B, mu, c);
         if (q == b) {
 #pragma unroll
             for (int m = 0; m < 9; m++) acc[m] = fix_zero(c[m]);
@@ -190,14 +232,14 @@ __global__ void __launch_bounds__(kThreads)
 k_weights64(const double *__restrict__ coef, int nbElem, double *__restrict__ rec) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nbElem) return;
-    double2 *out = reinterpret_cast<double2 *>(rec + (size_t)e * kRec64);
+    double *r = rec + (size_t)e * kRec64;
     if (OP == MFEM_OP_LAP) {
-        out[6] = make_double2(coef[e], 0.0);
+        const double kappa = coef[e];
+        r[3] = kappa; r[7] = kappa; r[11] = kappa; r[15] = kappa;
     } else {
         double A, B, mu;
         lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
-        out[6] = make_double2(A, B);
-        out[7] = make_double2(mu, 0.0);
+        r[3] = A; r[7] = B; r[11] = mu; r[15] = A;
     }
 }
 
@@ -215,22 +257,21 @@ k_elem_scatter64(const int *__restrict__ elems, int count, const double *__restr
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long item = t >> 4;
     if (item >= count) return;
-    const int jk = (int)(t & 15), j = jk >> 2, k = jk & 3;
+    const int jk = (int)(t & 15);
+    const unsigned j = jk >> 2, k = jk & 3;
     const int e = elems[item];
     const double *r = rec + (size_t)e * kRec64;
     const int p = elemPos[(size_t)e * 16 + jk];
+    double gj[3], gk[3];
+    const double wj = ld_chunk(r, j, gj), wk = ld_chunk(r, k, gk);
     if (OP == MFEM_OP_LAP) {
-        const double v = lap_entry<!COEF>(r + 3 * j, r + 3 * k, COEF ? r[12] : 1.0);
+        const double v = lap_entry<!COEF, kSplitEdge>(gj, gk, wj);
         values[p] = values[p] + v;
     } else {
         double A = 2.25, B = 1.25, mu = 1.0;
-        if (COEF) {
-            A = r[12];
-            B = r[13];
-            mu = r[14];
-        }
+        if (COEF) ela_weights(r, j, wj, k, wk, A, B, mu);
         double c[9];
-        ela_block<!COEF>(r + 3 * j, r + 3 * k, A, B, mu, c);
+        ela_block<!COEF, kSplitEdge>(gj, gk, A, B, mu, c);
         double *v = values + (size_t)p * 9;
 #pragma unroll
         for (int m = 0; m < 9; m++) v[m] = v[m] + c[m];
@@ -248,7 +289,7 @@ k_elem_atomic64(const int *__restrict__ elems, int count, const double *__restri
     if (t >= count) return;
     const int e = elems ? elems[t] : t;
     double g[12];
-    elem_gradients(coord, e2n[e], g);
+    elem_gradients<kSplitGrad>(coord, e2n[e], g);
     double A = 2.25, B = 1.25, mu = 1.0, kappa = 1.0;
     if (COEF) {
         if (OP == MFEM_OP_LAP) kappa = coef[e];
@@ -261,12 +302,12 @@ k_elem_atomic64(const int *__restrict__ elems, int count, const double *__restri
         for (int k = j; k < 4; k++) {
             const int pjk = pos[4 * j + k], pkj = pos[4 * k + j];
             if (OP == MFEM_OP_LAP) {
-                const double v = lap_entry<!COEF>(g + 3 * j, g + 3 * k, kappa);
+                const double v = lap_entry<!COEF, kSplitEdge>(g + 3 * j, g + 3 * k, kappa);
                 atomicAdd(values + pjk, v);
                 if (k != j) atomicAdd(values + pkj, v);
             } else {
                 double c[9];
-                ela_block<!COEF>(g + 3 * j, g + 3 * k, A, B, mu, c);
+                ela_block<!COEF, kSplitEdge>(g + 3 * j, g + 3 * k, A, B, mu, c);
                 double *vj = values + (size_t)pjk * 9;
                 double *vk = values + (size_t)pkj * 9;
 #pragma unroll
@@ -343,12 +384,12 @@ void launch_gather(Context &c, bool fusePrec) {
     c.timer.begin(fusePrec ? "diag_units64+prec" : "diag_units64", c.stream);
     if (fusePrec)
         k_diag_units64<OP, COEF, true><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(
-            c.diagPos.as<int>(), g.unitStart.as<int>(), g.contrib.as<unsigned>(), rec, N, vals,
-            prec, mask, sing);
+            g.diagNode.as<int>(), c.diagPos.as<int>(), g.unitStart.as<int>(),
+            g.contrib.as<unsigned>(), rec, N, vals, prec, mask, sing);
     else
         k_diag_units64<OP, COEF, false><<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(
-            c.diagPos.as<int>(), g.unitStart.as<int>(), g.contrib.as<unsigned>(), rec, N, vals,
-            prec, mask, sing);
+            g.diagNode.as<int>(), c.diagPos.as<int>(), g.unitStart.as<int>(),
+            g.contrib.as<unsigned>(), rec, N, vals, prec, mask, sing);
     check_launch("k_diag_units64");
     c.timer.end(c.stream);
     if (g.nUnits > 0) {
@@ -454,31 +495,31 @@ void gather_fp64_into(const Context &c, int op, const double *coord, const doubl
                       double *rec, double *values, cudaStream_t s) {
     const GatherPlan &g = c.gather;
     const int E = c.nbElem, N = c.nbNodes;
-    const int *dp = c.diagPos.as<int>(), *st = g.unitStart.as<int>();
+    const int *dp = c.diagPos.as<int>(), *st = g.unitStart.as<int>(), *dn = g.diagNode.as<int>();
     const unsigned *ct = g.contrib.as<unsigned>();
     const int2 *up = g.unitPos.as<int2>();
     const int4 *e2n = c.e2n.as<int4>();
     if (op == MFEM_OP_LAP) {
         if (coef) {
             k_grad64<MFEM_OP_LAP, true><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
-            k_diag_units64<MFEM_OP_LAP, true, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            k_diag_units64<MFEM_OP_LAP, true, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dn, dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
             if (g.nUnits > 0)
                 k_edge_units64<MFEM_OP_LAP, true><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
         } else {
             k_grad64<MFEM_OP_LAP, false><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, nullptr, E, rec);
-            k_diag_units64<MFEM_OP_LAP, false, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            k_diag_units64<MFEM_OP_LAP, false, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dn, dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
             if (g.nUnits > 0)
                 k_edge_units64<MFEM_OP_LAP, false><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
         }
     } else {
         if (coef) {
             k_grad64<MFEM_OP_ELA, true><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
-            k_diag_units64<MFEM_OP_ELA, true, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            k_diag_units64<MFEM_OP_ELA, true, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dn, dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
             if (g.nUnits > 0)
                 k_edge_units64<MFEM_OP_ELA, true><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
         } else {
             k_grad64<MFEM_OP_ELA, false><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, nullptr, E, rec);
-            k_diag_units64<MFEM_OP_ELA, false, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            k_diag_units64<MFEM_OP_ELA, false, false><<<blocks_for(N, kThreads), kThreads, 0, s>>>(dn, dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
             if (g.nUnits > 0)
                 k_edge_units64<MFEM_OP_ELA, false><<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
         }
@@ -494,7 +535,7 @@ void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec,
                       bool gradientsReady) {
     const GatherPlan &g = c.gather;
     const int E = c.nbElem, N = c.nbNodes;
-    const int *dp = c.diagPos.as<int>(), *st = g.unitStart.as<int>();
+    const int *dp = c.diagPos.as<int>(), *st = g.unitStart.as<int>(), *dn = g.diagNode.as<int>();
     const unsigned *ct = g.contrib.as<unsigned>();
     const int2 *up = g.unitPos.as<int2>();
     const int4 *e2n = c.e2n.as<int4>();
@@ -509,9 +550,9 @@ void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec,
             else k_weights64<MFEM_OP_ELA><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coef, E, rec);
         }
         if (prec)
-            diagp<<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, prec, mask, singular);
+            diagp<<<blocks_for(N, kThreads), kThreads, 0, s>>>(dn, dp, st, ct, rec, N, values, prec, mask, singular);
         else
-            diag<<<blocks_for(N, kThreads), kThreads, 0, s>>>(dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
+            diag<<<blocks_for(N, kThreads), kThreads, 0, s>>>(dn, dp, st, ct, rec, N, values, nullptr, nullptr, nullptr);
         if (g.nUnits > 0)
             edge<<<blocks_for(g.nUnits, kThreads), kThreads, 0, s>>>(up, g.nUnits, st, ct, rec, values);
     };

@@ -22,10 +22,10 @@ struct GatherPlan {
     int nUnits = 0;
     long long nContrib = 0;
     DevBuf unitStart;   // int [nUnits + 1]  offsets into contrib (in unit order)
-    DevBuf unitPos;     // int2[nUnits]      (pos(r,c), pos(c,r))
+    DevBuf unitPos;     // int2[nUnits]      (pos(r,c), pos(c,r)), by first element, then count
     DevBuf contrib;     // u32 [nContrib]
     int nDiagUnits = 0; // units [0, nDiagUnits) are diagonal entries
-    DevBuf diagNode;    // int [nDiagUnits]  node of each diagonal unit
+    DevBuf diagNode;    // int [nDiagUnits]  nodes by first incident element, then valence
 };
 
 // FP32 spatial-tile plan (tiles.cu): rows in Morton order cut into tiles of at

@@ -5,10 +5,31 @@
 
 #include <cuda_runtime.h>
 
+#include "dmul_int.cuh"
+
 namespace mfem {
 
-// Per-element gradient record: g_j (j = 0..3) at [3j, 3j+3), then the weights
-// (A, B, mu) for ela or kappa for lap, 16 doubles = 128 bytes.
+// Multiply split: which products of a formula go to the integer pipes
+// (dmul_ipipe) and which to the FP64 unit.  Both give the same bits, so a split
+// only balances the two pipes; each kernel picks its own (a template argument).
+enum : int {
+    kIntGrad = 1,    // g_j[a] * g_k[b] in the blocks
+    kIntDiagW = 2,   // p_aa * (A or mu)
+    kIntOffW = 4,    // p_ab * B
+    kIntCross = 8,   // cross products of the edge vectors
+    kIntScale = 16,  // gradients times 1/vol
+};
+
+template <bool INT>
+__device__ __forceinline__ double dmul(double a, double b) {
+    if constexpr (INT) return dmul_ipipe(a, b);
+    else return a * b;
+}
+
+// Per-element gradient record, 16 doubles = 128 bytes in four 32-byte chunks
+// (g_j.x, g_j.y, g_j.z, w_j), so that one 256-bit load brings a gradient and a
+// weight.  The weights sit in the spare slots: ela w = (A, B, mu, A), lap
+// w = (kappa, kappa, kappa, kappa).
 constexpr int kRec64 = 16;
 
 __device__ __forceinline__ double neg(double x) {
@@ -19,6 +40,7 @@ __device__ __forceinline__ double neg(double x) {
 // assembly.cc:85-121 elem_coef_seq: gradients of the barycentric coordinates
 // scaled by the reciprocal of the signed 6*volume.  Note the reference's b/c
 // order: xb = n2 - n3, xc = n1 - n3.
+template <int SPLIT = 0>
 __device__ __forceinline__ void elem_gradients(const double *__restrict__ coord, int4 nd,
                                                double g[12]) {
     const double x0 = coord[3 * nd.x], y0 = coord[3 * nd.x + 1], z0 = coord[3 * nd.x + 2];
@@ -28,18 +50,23 @@ __device__ __forceinline__ void elem_gradients(const double *__restrict__ coord,
     const double xa = x0 - x3, xb = x2 - x3, xc = x1 - x3;
     const double ya = y0 - y3, yb = y2 - y3, yc = y1 - y3;
     const double za = z0 - z3, zb = z2 - z3, zc = z1 - z3;
-    const double g00 = yb * zc - yc * zb, g01 = zb * xc - zc * xb, g02 = xb * yc - xc * yb;
-    const double g10 = ya * zb - yb * za, g11 = za * xb - zb * xa, g12 = xa * yb - xb * ya;
-    const double g20 = yc * za - ya * zc, g21 = zc * xa - za * xc, g22 = xc * ya - xa * yc;
+    constexpr bool X = (SPLIT & kIntCross) != 0;
+    const double g00 = dmul<X>(yb, zc) - dmul<X>(yc, zb), g01 = dmul<X>(zb, xc) - dmul<X>(zc, xb),
+                 g02 = dmul<X>(xb, yc) - dmul<X>(xc, yb);
+    const double g10 = dmul<X>(ya, zb) - dmul<X>(yb, za), g11 = dmul<X>(za, xb) - dmul<X>(zb, xa),
+                 g12 = dmul<X>(xa, yb) - dmul<X>(xb, ya);
+    const double g20 = dmul<X>(yc, za) - dmul<X>(ya, zc), g21 = dmul<X>(zc, xa) - dmul<X>(za, xc),
+                 g22 = dmul<X>(xc, ya) - dmul<X>(xa, yc);
     const double g30 = neg((g00 + g10) + g20);
     const double g31 = neg((g01 + g11) + g21);
     const double g32 = neg((g02 + g12) + g22);
     const double vol = (xa * g00 + ya * g01) + za * g02;
     const double r = 1.0 / vol;
-    g[0] = g00 * r; g[1] = g01 * r; g[2] = g02 * r;
-    g[3] = g10 * r; g[4] = g11 * r; g[5] = g12 * r;
-    g[6] = g20 * r; g[7] = g21 * r; g[8] = g22 * r;
-    g[9] = g30 * r; g[10] = g31 * r; g[11] = g32 * r;
+    constexpr bool S = (SPLIT & kIntScale) != 0;
+    g[0] = dmul<S>(g00, r); g[1] = dmul<S>(g01, r); g[2] = dmul<S>(g02, r);
+    g[3] = dmul<S>(g10, r); g[4] = dmul<S>(g11, r); g[5] = dmul<S>(g12, r);
+    g[6] = dmul<S>(g20, r); g[7] = dmul<S>(g21, r); g[8] = dmul<S>(g22, r);
+    g[9] = dmul<S>(g30, r); g[10] = dmul<S>(g31, r); g[11] = dmul<S>(g32, r);
 }
 
 // Lame weights from Young's modulus and Poisson ratio; A = lambda + 2 mu,
@@ -57,61 +84,71 @@ __device__ __forceinline__ void lame_weights(double E, double nu, double &A, dou
 //   c(a,a) = ((p00*w0 + p11*w1) + p22*w2) with w = A on the a-th term, mu else
 //   c(a,b) = p_ab * B
 // (assembly.cc:423-446; the reference's constants are A = 2.25, B = 1.25, mu = 1).
-template <bool REFW>
+template <bool REFW, int SPLIT = 0>
 __device__ __forceinline__ void ela_block(const double *gj, const double *gk, double A,
                                           double B, double mu, double c[9]) {
-    const double p00 = gj[0] * gk[0], p11 = gj[1] * gk[1], p22 = gj[2] * gk[2];
+    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagW) != 0,
+                   O = (SPLIT & kIntOffW) != 0;
+    const double p00 = dmul<G>(gj[0], gk[0]), p11 = dmul<G>(gj[1], gk[1]),
+                 p22 = dmul<G>(gj[2], gk[2]);
+    const double p01 = dmul<G>(gj[0], gk[1]), p02 = dmul<G>(gj[0], gk[2]),
+                 p10 = dmul<G>(gj[1], gk[0]), p12 = dmul<G>(gj[1], gk[2]),
+                 p20 = dmul<G>(gj[2], gk[0]), p21 = dmul<G>(gj[2], gk[1]);
     if (REFW) {
-        c[0] = (p00 * 2.25 + p11) + p22;
-        c[4] = (p00 + p11 * 2.25) + p22;
-        c[8] = (p00 + p11) + p22 * 2.25;
-        c[1] = (gj[0] * gk[1]) * 1.25;
-        c[2] = (gj[0] * gk[2]) * 1.25;
-        c[3] = (gj[1] * gk[0]) * 1.25;
-        c[5] = (gj[1] * gk[2]) * 1.25;
-        c[6] = (gj[2] * gk[0]) * 1.25;
-        c[7] = (gj[2] * gk[1]) * 1.25;
+        c[0] = (dmul<W>(p00, 2.25) + p11) + p22;
+        c[4] = (p00 + dmul<W>(p11, 2.25)) + p22;
+        c[8] = (p00 + p11) + dmul<W>(p22, 2.25);
+        c[1] = dmul<O>(p01, 1.25);
+        c[2] = dmul<O>(p02, 1.25);
+        c[3] = dmul<O>(p10, 1.25);
+        c[5] = dmul<O>(p12, 1.25);
+        c[6] = dmul<O>(p20, 1.25);
+        c[7] = dmul<O>(p21, 1.25);
     } else {
-        c[0] = (p00 * A + p11 * mu) + p22 * mu;
-        c[4] = (p00 * mu + p11 * A) + p22 * mu;
-        c[8] = (p00 * mu + p11 * mu) + p22 * A;
-        c[1] = (gj[0] * gk[1]) * B;
-        c[2] = (gj[0] * gk[2]) * B;
-        c[3] = (gj[1] * gk[0]) * B;
-        c[5] = (gj[1] * gk[2]) * B;
-        c[6] = (gj[2] * gk[0]) * B;
-        c[7] = (gj[2] * gk[1]) * B;
+        c[0] = (dmul<W>(p00, A) + dmul<W>(p11, mu)) + dmul<W>(p22, mu);
+        c[4] = (dmul<W>(p00, mu) + dmul<W>(p11, A)) + dmul<W>(p22, mu);
+        c[8] = (dmul<W>(p00, mu) + dmul<W>(p11, mu)) + dmul<W>(p22, A);
+        c[1] = dmul<O>(p01, B);
+        c[2] = dmul<O>(p02, B);
+        c[3] = dmul<O>(p10, B);
+        c[5] = dmul<O>(p12, B);
+        c[6] = dmul<O>(p20, B);
+        c[7] = dmul<O>(p21, B);
     }
 }
 
 // Diagonal block (j,j): symmetric bit for bit, six distinct values
 // (c0, c4, c8, c1 = c3, c2 = c6, c5 = c7).
-template <bool REFW>
+template <bool REFW, int SPLIT = 0>
 __device__ __forceinline__ void ela_diag_block(const double *g, double A, double B,
                                                double mu, double d[6]) {
-    const double p00 = g[0] * g[0], p11 = g[1] * g[1], p22 = g[2] * g[2];
+    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagW) != 0,
+                   O = (SPLIT & kIntOffW) != 0;
+    const double p00 = dmul<G>(g[0], g[0]), p11 = dmul<G>(g[1], g[1]), p22 = dmul<G>(g[2], g[2]);
+    const double p01 = dmul<G>(g[0], g[1]), p02 = dmul<G>(g[0], g[2]), p12 = dmul<G>(g[1], g[2]);
     if (REFW) {
-        d[0] = (p00 * 2.25 + p11) + p22;
-        d[1] = (p00 + p11 * 2.25) + p22;
-        d[2] = (p00 + p11) + p22 * 2.25;
-        d[3] = (g[0] * g[1]) * 1.25;
-        d[4] = (g[0] * g[2]) * 1.25;
-        d[5] = (g[1] * g[2]) * 1.25;
+        d[0] = (dmul<W>(p00, 2.25) + p11) + p22;
+        d[1] = (p00 + dmul<W>(p11, 2.25)) + p22;
+        d[2] = (p00 + p11) + dmul<W>(p22, 2.25);
+        d[3] = dmul<O>(p01, 1.25);
+        d[4] = dmul<O>(p02, 1.25);
+        d[5] = dmul<O>(p12, 1.25);
     } else {
-        d[0] = (p00 * A + p11 * mu) + p22 * mu;
-        d[1] = (p00 * mu + p11 * A) + p22 * mu;
-        d[2] = (p00 * mu + p11 * mu) + p22 * A;
-        d[3] = (g[0] * g[1]) * B;
-        d[4] = (g[0] * g[2]) * B;
-        d[5] = (g[1] * g[2]) * B;
+        d[0] = (dmul<W>(p00, A) + dmul<W>(p11, mu)) + dmul<W>(p22, mu);
+        d[1] = (dmul<W>(p00, mu) + dmul<W>(p11, A)) + dmul<W>(p22, mu);
+        d[2] = (dmul<W>(p00, mu) + dmul<W>(p11, mu)) + dmul<W>(p22, A);
+        d[3] = dmul<O>(p01, B);
+        d[4] = dmul<O>(p02, B);
+        d[5] = dmul<O>(p12, B);
     }
 }
 
 // assembly.cc:555-557: (gj0*gk0 + gj1*gk1) + gj2*gk2, weighted by kappa.
-template <bool REFW>
+template <bool REFW, int SPLIT = 0>
 __device__ __forceinline__ double lap_entry(const double *gj, const double *gk, double kappa) {
-    const double s = (gj[0] * gk[0] + gj[1] * gk[1]) + gj[2] * gk[2];
-    return REFW ? s : kappa * s;
+    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagW) != 0;
+    const double s = (dmul<G>(gj[0], gk[0]) + dmul<G>(gj[1], gk[1])) + dmul<G>(gj[2], gk[2]);
+    return REFW ? s : dmul<W>(kappa, s);
 }
 
 // DLAMCH('S'): smallest normal double.

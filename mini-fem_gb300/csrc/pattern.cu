@@ -307,46 +307,64 @@ __global__ void k_plan_fill(const int *__restrict__ ptr, const int *__restrict__
     }
 }
 
-// Off-diagonal upper units, bucketed by contribution count so that a warp
-// processes lists of equal length.
-__global__ void k_unit_hist(const int *__restrict__ rowOf, const int *__restrict__ col,
-                            const int *__restrict__ start, int nnz, int *hist) {
+// Units in element-locality order.  A unit's key is its first (smallest)
+// contributing element, in windows of 512 elements, then its contribution count:
+// the warps of a window read gradient records of nearby elements (which the L2
+// keeps), and most of them loop the same number of times.  Placement within a
+// key is in atomic order, which changes where a unit runs but not its sum.
+constexpr int kOwnerShift = 9;
+constexpr int kUnitCountBins = 16;
+constexpr int kDiagCountBins = 32;
+
+__global__ void k_unit_key(const int *__restrict__ rowOf, const int *__restrict__ col,
+                           const int *__restrict__ start, const unsigned *__restrict__ contrib,
+                           int nnz, int *key, int *keyCount) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nnz) return;
-    int r = rowOf[p];
-    if (col[p] <= r) return;
-    int n = start[p + 1] - start[p];
-    atomicAdd(&hist[min(n, 63)], 1);
+    if (col[p] <= rowOf[p]) {
+        key[p] = -1;
+        return;
+    }
+    const int n = start[p + 1] - start[p];
+    const unsigned owner = n > 0 ? contrib[start[p]] >> 4 : 0u;
+    const int k = (int)(owner >> kOwnerShift) * kUnitCountBins + min(max(n, 1) - 1, kUnitCountBins - 1);
+    key[p] = k;
+    atomicAdd(&keyCount[k], 1);
 }
 
-__global__ void k_unit_place(const int *__restrict__ rowOf, const int *__restrict__ col,
-                             const int *__restrict__ start, const int *__restrict__ tpos,
-                             int nnz, int *bucketFill, int2 *unitPos) {
+__global__ void k_unit_place(const int *__restrict__ key, const int *__restrict__ tpos, int nnz,
+                             int *keyFill, int2 *unitPos) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nnz) return;
-    int r = rowOf[p];
-    if (col[p] <= r) return;
-    int n = start[p + 1] - start[p];
-    // descending count: bucket 63 first
-    int slot = atomicAdd(&bucketFill[63 - min(n, 63)], 1);
-    unitPos[slot] = make_int2(p, tpos[p]);
+    const int k = key[p];
+    if (k < 0) return;
+    unitPos[atomicAdd(&keyFill[k], 1)] = make_int2(p, tpos[p]);
+}
+
+// Diagonal units (one per node) keyed the same way by the node's first
+// incident element and its number of incident elements.
+__global__ void k_diag_key(const int *__restrict__ ptr, const int *__restrict__ nodeElem,
+                           int nbNodes, int *key, int *keyCount) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    const int n = ptr[r + 1] - ptr[r];
+    const unsigned owner = n > 0 ? (unsigned)nodeElem[ptr[r]] >> 2 : 0u;
+    const int k = (int)(owner >> kOwnerShift) * kDiagCountBins + min(max(n, 1) - 1, kDiagCountBins - 1);
+    key[r] = k;
+    atomicAdd(&keyCount[k], 1);
+}
+
+__global__ void k_diag_place(const int *__restrict__ key, int nbNodes, int *keyFill,
+                             int *diagNode) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nbNodes) return;
+    diagNode[atomicAdd(&keyFill[key[r]], 1)] = r;
 }
 
 __global__ void k_row_of(const int *__restrict__ rowPtr, int nbNodes, int *rowOf) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nbNodes) return;
     for (int p = rowPtr[r]; p < rowPtr[r + 1]; p++) rowOf[p] = r;
-}
-
-__global__ void k_reverse_hist_offsets(const int *hist, int *fill) {
-    // fill[b] = start of bucket (63 - b) in descending-count order
-    if (threadIdx.x == 0) {
-        int s = 0;
-        for (int b = 0; b < 64; b++) {
-            fill[b] = s;
-            s += hist[63 - b];
-        }
-    }
 }
 
 void check_status(Context &c, const char *what) {
@@ -529,12 +547,16 @@ void build_gather_plan(Context &c) {
     GatherPlan &g = c.gather;
     int *st = status_ptr(c);
     MFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(int), c.stream));
-    // scratch layout: rowOf[nnz] | fill[nnz] | tpos[nnz] | hist[64] | bfill[64]
-    int *work = (int *)c.scratch2.reserve(sizeof(int) * ((size_t)nnz * 3 + 128));
-    int *rowOf = work, *fill = work + nnz, *tpos = work + 2LL * nnz;
-    int *hist = work + 3LL * nnz, *bfill = hist + 64;
+    // scratch layout: rowOf[nnz] | fill[max(nnz, N)] (then unit / node keys) |
+    // tpos[nnz] | keyCount[nKeys + 1]
+    const long long nKeys = ((long long)(c.nbElem >> kOwnerShift) + 1) * kDiagCountBins;
+    MFEM_REQUIRE(nKeys < (1LL << 31), MFEM_ERR_CAPACITY, "gather plan: too many elements");
+    const size_t nFill = std::max<size_t>((size_t)nnz, (size_t)N);
+    int *work = (int *)c.scratch2.reserve(sizeof(int) * ((size_t)nnz * 2 + nFill + (size_t)nKeys + 1));
+    int *rowOf = work, *fill = work + nnz, *tpos = fill + nFill;
+    int *keyCount = tpos + nnz;
     int *start = (int *)g.unitStart.reserve(sizeof(int) * ((size_t)nnz + 1));
-    int *tmp = (int *)c.scanTmp.reserve(sizeof(int) * scan_tmp_elems(nnz + 1));
+    int *tmp = (int *)c.scanTmp.reserve(sizeof(int) * scan_tmp_elems(std::max<long long>(nnz, nKeys) + 1));
     const int *ptr = c.nodeElemPtr.as<int>(), *ne = c.nodeElem.as<int>(), *e2n = c.e2n.as<int>();
     const int *rowPtr = c.rowPtr.as<int>(), *col = c.col.as<int>();
 
@@ -551,18 +573,27 @@ void build_gather_plan(Context &c) {
     check_launch("k_plan_fill");
     k_row_of<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(rowPtr, N, rowOf);
     check_launch("k_row_of");
-    MFEM_CUDA(cudaMemsetAsync(hist, 0, sizeof(int) * 128, c.stream));
-    k_unit_hist<<<blocks_for(nnz, kThreads), kThreads, 0, c.stream>>>(rowOf, col, start, nnz, hist);
-    check_launch("k_unit_hist");
-    int hh[64];
-    MFEM_CUDA(cudaMemcpyAsync(hh, hist, sizeof(hh), cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaStreamSynchronize(c.stream));
+    // off-diagonal units
+    const int nKeysU = (int)(nKeys / kDiagCountBins * kUnitCountBins);
+    int *key = fill;
+    MFEM_CUDA(cudaMemsetAsync(keyCount, 0, sizeof(int) * ((size_t)nKeysU + 1), c.stream));
+    k_unit_key<<<blocks_for(nnz, kThreads), kThreads, 0, c.stream>>>(rowOf, col, start, contrib, nnz, key, keyCount);
+    check_launch("k_unit_key");
+    exclusive_scan_i32(keyCount, keyCount, nKeysU, tmp, c.stream);
     int nEdge = 0;
-    for (int b = 0; b < 64; b++) nEdge += hh[b];
-    k_reverse_hist_offsets<<<1, 32, 0, c.stream>>>(hist, bfill);
+    MFEM_CUDA(cudaMemcpyAsync(&nEdge, keyCount + nKeysU, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    MFEM_CUDA(cudaStreamSynchronize(c.stream));
     int2 *upos = (int2 *)g.unitPos.reserve(sizeof(int2) * (size_t)(nEdge > 0 ? nEdge : 1));
-    k_unit_place<<<blocks_for(nnz, kThreads), kThreads, 0, c.stream>>>(rowOf, col, start, tpos, nnz, bfill, upos);
+    k_unit_place<<<blocks_for(nnz, kThreads), kThreads, 0, c.stream>>>(key, tpos, nnz, keyCount, upos);
     check_launch("k_unit_place");
+    // diagonal units
+    int *dnode = (int *)g.diagNode.reserve(sizeof(int) * (size_t)N);
+    MFEM_CUDA(cudaMemsetAsync(keyCount, 0, sizeof(int) * ((size_t)nKeys + 1), c.stream));
+    k_diag_key<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(ptr, ne, N, key, keyCount);
+    check_launch("k_diag_key");
+    exclusive_scan_i32(keyCount, keyCount, nKeys, tmp, c.stream);
+    k_diag_place<<<blocks_for(N, kThreads), kThreads, 0, c.stream>>>(key, N, keyCount, dnode);
+    check_launch("k_diag_place");
     check_status(c, "gather plan");
     g.nUnits = nEdge;
     g.nContrib = total;

@@ -178,6 +178,13 @@ class Assembler:
         return {"tiles": t.value, "tile_elems": e.value, "units": u.value,
                 "contributions": k.value, "smem_bytes": s.value}
 
+    def selftest_dmul(self, n: int, seed: int = 1) -> tuple[int, int]:
+        """(pairs on the fast path, mismatches) of the integer-pipe double
+        multiplication against the FP64 unit over n seeded operand pairs."""
+        f, m = C.c_ulonglong(), C.c_ulonglong()
+        self._check(N.lib.mfem_selftest_dmul(self._h, n, seed, C.byref(f), C.byref(m)))
+        return f.value, m.value
+
     def flagged(self) -> int:
         n = C.c_int()
         self._check(N.lib.mfem_get_flagged(self._h, C.byref(n)))
