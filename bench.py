@@ -140,12 +140,12 @@ def kernel_bytes(name, E, N, nnz, n_edge_units, fp32):
 
 
 # DRAM bytes per element of one launch, from `ncu --set full` captures of the 60^3
-# cube (profiles/tile32_ela_cube60.md, profiles/edge_units64_ela_cube60.md:
+# cube (profiles/tile32_ela_cube60.md, profiles/fp64_units_ela_cube60.md:
 # dram__bytes_read.sum + dram__bytes_write.sum divided by its 1,232,274 tets);
 # traffic grows in proportion to the mesh, so the full launch's traffic is this
 # times E.
 TRAFFIC_PER_ELEM = {"tile32+prec": (144.332288e6 + 94.564352e6) / 1232274,
-                    "edge_units64": (858.412288e6 + 245.096704e6) / 1232274}
+                    "edge_units64": (282.084864e6 + 198.790656e6) / 1232274}
 
 
 def make_mesh(rank):

@@ -14,10 +14,12 @@ namespace mfem {
 // only balances the two pipes; each kernel picks its own (a template argument).
 enum : int {
     kIntGrad = 1,    // g_j[a] * g_k[b] in the blocks
-    kIntDiagW = 2,   // p_aa * (A or mu)
+    kIntDiagA = 2,   // p_aa * A
     kIntOffW = 4,    // p_ab * B
     kIntCross = 8,   // cross products of the edge vectors
     kIntScale = 16,  // gradients times 1/vol
+    kIntDiagMu = 32, // p_aa * mu
+    kIntDiagW = kIntDiagA | kIntDiagMu,
 };
 
 template <bool INT>
@@ -87,8 +89,8 @@ __device__ __forceinline__ void lame_weights(double E, double nu, double &A, dou
 template <bool REFW, int SPLIT = 0>
 __device__ __forceinline__ void ela_block(const double *gj, const double *gk, double A,
                                           double B, double mu, double c[9]) {
-    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagW) != 0,
-                   O = (SPLIT & kIntOffW) != 0;
+    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagA) != 0,
+                   M = (SPLIT & kIntDiagMu) != 0, O = (SPLIT & kIntOffW) != 0;
     const double p00 = dmul<G>(gj[0], gk[0]), p11 = dmul<G>(gj[1], gk[1]),
                  p22 = dmul<G>(gj[2], gk[2]);
     const double p01 = dmul<G>(gj[0], gk[1]), p02 = dmul<G>(gj[0], gk[2]),
@@ -105,9 +107,9 @@ __device__ __forceinline__ void ela_block(const double *gj, const double *gk, do
         c[6] = dmul<O>(p20, 1.25);
         c[7] = dmul<O>(p21, 1.25);
     } else {
-        c[0] = (dmul<W>(p00, A) + dmul<W>(p11, mu)) + dmul<W>(p22, mu);
-        c[4] = (dmul<W>(p00, mu) + dmul<W>(p11, A)) + dmul<W>(p22, mu);
-        c[8] = (dmul<W>(p00, mu) + dmul<W>(p11, mu)) + dmul<W>(p22, A);
+        c[0] = (dmul<W>(p00, A) + dmul<M>(p11, mu)) + dmul<M>(p22, mu);
+        c[4] = (dmul<M>(p00, mu) + dmul<W>(p11, A)) + dmul<M>(p22, mu);
+        c[8] = (dmul<M>(p00, mu) + dmul<M>(p11, mu)) + dmul<W>(p22, A);
         c[1] = dmul<O>(p01, B);
         c[2] = dmul<O>(p02, B);
         c[3] = dmul<O>(p10, B);
@@ -122,8 +124,8 @@ __device__ __forceinline__ void ela_block(const double *gj, const double *gk, do
 template <bool REFW, int SPLIT = 0>
 __device__ __forceinline__ void ela_diag_block(const double *g, double A, double B,
                                                double mu, double d[6]) {
-    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagW) != 0,
-                   O = (SPLIT & kIntOffW) != 0;
+    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagA) != 0,
+                   M = (SPLIT & kIntDiagMu) != 0, O = (SPLIT & kIntOffW) != 0;
     const double p00 = dmul<G>(g[0], g[0]), p11 = dmul<G>(g[1], g[1]), p22 = dmul<G>(g[2], g[2]);
     const double p01 = dmul<G>(g[0], g[1]), p02 = dmul<G>(g[0], g[2]), p12 = dmul<G>(g[1], g[2]);
     if (REFW) {
@@ -134,9 +136,9 @@ __device__ __forceinline__ void ela_diag_block(const double *g, double A, double
         d[4] = dmul<O>(p02, 1.25);
         d[5] = dmul<O>(p12, 1.25);
     } else {
-        d[0] = (dmul<W>(p00, A) + dmul<W>(p11, mu)) + dmul<W>(p22, mu);
-        d[1] = (dmul<W>(p00, mu) + dmul<W>(p11, A)) + dmul<W>(p22, mu);
-        d[2] = (dmul<W>(p00, mu) + dmul<W>(p11, mu)) + dmul<W>(p22, A);
+        d[0] = (dmul<W>(p00, A) + dmul<M>(p11, mu)) + dmul<M>(p22, mu);
+        d[1] = (dmul<M>(p00, mu) + dmul<W>(p11, A)) + dmul<M>(p22, mu);
+        d[2] = (dmul<M>(p00, mu) + dmul<M>(p11, mu)) + dmul<W>(p22, A);
         d[3] = dmul<O>(p01, B);
         d[4] = dmul<O>(p02, B);
         d[5] = dmul<O>(p12, B);
@@ -146,7 +148,7 @@ __device__ __forceinline__ void ela_diag_block(const double *g, double A, double
 // assembly.cc:555-557: (gj0*gk0 + gj1*gk1) + gj2*gk2, weighted by kappa.
 template <bool REFW, int SPLIT = 0>
 __device__ __forceinline__ double lap_entry(const double *gj, const double *gk, double kappa) {
-    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagW) != 0;
+    constexpr bool G = (SPLIT & kIntGrad) != 0, W = (SPLIT & kIntDiagA) != 0;
     const double s = (dmul<G>(gj[0], gk[0]) + dmul<G>(gj[1], gk[1])) + dmul<G>(gj[2], gk[2]);
     return REFW ? s : dmul<W>(kappa, s);
 }
