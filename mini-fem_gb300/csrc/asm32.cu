@@ -28,9 +28,14 @@ __global__ void k_split_coords(const double *__restrict__ coord, int nbNodes,
                         __double2float_rn(z - (double)zh), 0.f);
 }
 
-__global__ void k_coef_to_f32(const double *__restrict__ in, long long n, float *__restrict__ out) {
+// FP32 coefficients of the record kernel: kappa (lap) or (E, 1/2 - nu) (ela,
+// the form lame32 takes; the subtraction in FP64).
+__global__ void k_coef_to_f32(const double *__restrict__ in, long long n, int perElem,
+                              float *__restrict__ out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = __double2float_rn(in[i]);
+    if (i >= n) return;
+    const bool nuSlot = perElem == 2 && (i & 1);
+    out[i] = __double2float_rn(nuSlot ? 0.5 - in[i] : in[i]);
 }
 
 // a*b - c*d with one rounding error less than the plain expression (Kahan).
@@ -91,11 +96,10 @@ k_grad32(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
         if (OP == MFEM_OP_LAP) {
             A = coef[e];
         } else {
-            const float E = coef[2 * (size_t)e], nu = coef[2 * (size_t)e + 1];
-            const float lam = (E * nu) / ((1.0f + nu) * (1.0f - 2.0f * nu));
-            mu = E / (2.0f * (1.0f + nu));
-            A = fmaf(2.0f, mu, lam);
-            B = lam + mu;
+            const float2 w = lame32(coef[2 * (size_t)e], coef[2 * (size_t)e + 1]);
+            B = w.x;
+            mu = w.y;
+            A = B + mu;
         }
     } else if (OP == MFEM_OP_LAP) {
         A = 1.0f;
@@ -249,7 +253,8 @@ void launch32(Context &c, bool fusePrec) {
         const long long n = (long long)E * (OP == MFEM_OP_LAP ? 1 : 2);
         float *cf = (float *)c.scratch2.reserve(sizeof(float) * n);
         c.timer.begin("coef_to_f32", c.stream);
-        k_coef_to_f32<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.coef.as<double>(), n, cf);
+        k_coef_to_f32<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.coef.as<double>(), n,
+                                                                  OP == MFEM_OP_LAP ? 1 : 2, cf);
         check_launch("k_coef_to_f32");
         c.timer.end(c.stream);
         coef = cf;

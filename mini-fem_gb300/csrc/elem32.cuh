@@ -59,12 +59,15 @@ __device__ __forceinline__ bool grad32_core(const ElemCoords &C, float qthr2, fl
     return false;
 }
 
-// Gradients of a flagged element: the FP64 formula, rounded to FP32.
+__device__ __forceinline__ float f64_to_f32(double x);
+
+// Gradients of a flagged element: the FP64 formula (its cross products and
+// 1/vol scalings on the integer pipes, elem_math.cuh), rounded to FP32.
 __device__ __forceinline__ void grad32_fp64(const double *__restrict__ coord, int4 nd, float g[12]) {
     double gd[12];
     elem_gradients(coord, nd, gd);
 #pragma unroll
-    for (int i = 0; i < 12; i++) g[i] = __double2float_rn(gd[i]);
+    for (int i = 0; i < 12; i++) g[i] = f64_to_f32(gd[i]);
 }
 
 // grad32_core, with flagged elements computed in FP64 from `coord`; returns
@@ -108,18 +111,15 @@ __device__ __forceinline__ double f32_to_f64(float x) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
-// Weights of the FP32 blocks: (B, mu) = (lambda + mu, mu) for ela, (kappa, 0)
-// for lap, in FP32 from the FP64 per-element coefficients (NULL: the reference
-// constants B = 1.25, mu = 1, kappa = 1).
+// Weights of the FP32 blocks: (B, mu) for ela, (kappa, 0) for lap, from the FP64
+// per-element coefficients (NULL: the reference constants B = 1.25, mu = 1,
+// kappa = 1).  One FP64 subtraction per element (1/2 - nu).
 template <int OP>
 __device__ __forceinline__ float2 weights32(const double *__restrict__ coef, int e) {
     if (OP == MFEM_OP_LAP) return make_float2(coef ? f64_to_f32(coef[e]) : 1.0f, 0.f);
     if (!coef) return make_float2(1.25f, 1.0f);
     const double2 c = reinterpret_cast<const double2 *>(coef)[e];
-    const float E = f64_to_f32(c.x), nu = f64_to_f32(c.y);
-    const float lam = (E * nu) / ((1.0f + nu) * (1.0f - 2.0f * nu));
-    const float mu = E / (2.0f * (1.0f + nu));
-    return make_float2(lam + mu, mu);
+    return lame32(f64_to_f32(c.x), f64_to_f32(0.5 - c.y));
 }
 
 struct Kahan {

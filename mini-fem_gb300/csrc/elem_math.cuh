@@ -153,6 +153,17 @@ __device__ __forceinline__ double lap_entry(const double *gj, const double *gk, 
     return REFW ? s : dmul<W>(kappa, s);
 }
 
+// Lame weights (B, mu) = (lambda + mu, mu) in FP32 from Young's modulus E and
+// h = 1/2 - nu, rounded to FP32 from its FP64 value: then 1 - 2 nu = 2h, 1 + nu =
+// 3/2 - h and nu = 1/2 - h carry no cancellation, where 1 - 2 nu formed from an
+// FP32 nu near 1/2 loses digits (its relative error grows as 1 / (1 - 2 nu)).
+__device__ __forceinline__ float2 lame32(float E, float h) {
+    const float nu = 0.5f - h, onePlus = 1.5f - h;
+    const float lam = (E * nu) / (onePlus * (2.0f * h));
+    const float mu = E / (2.0f * onePlus);
+    return make_float2(lam + mu, mu);
+}
+
 // DLAMCH('S'): smallest normal double.
 constexpr double kSafeMin = 2.2250738585072014e-308;
 

@@ -232,7 +232,9 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     int2 *sDiag = reinterpret_cast<int2 *>(sm + L.diag);
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);           // two barriers
     const int tid = threadIdx.x, lane = tid & 31;
-    __shared__ int sNext;   // next off-diagonal unit of phase 2
+    __shared__ int sNext;      // next off-diagonal unit of phase 2
+    __shared__ int sFlagged;   // elements of phase 1b queued for the FP64 gradients
+    if (tid == 0) sFlagged = 0;
 
     // 0. stage the entry tables with the TMA engine (barrier 0)
     if (tid == 0) {
@@ -274,24 +276,38 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     cp_async_wait_all();
     __syncthreads();
 
-    // 1b. gradients of the tile's elements
-    int flagged = 0;
+    // 1b. gradients of the tile's elements; flagged elements are queued (in
+    //     the row-result region, unused until phase 3a) and get their FP64
+    //     gradients in a second pass by consecutive threads, so that the FP64
+    //     work is spread over full warps instead of stalling every warp that
+    //     holds one flagged element
+    unsigned short *sFlag = reinterpret_cast<unsigned short *>(sm + L.res);
     for (int i = tid; i < T.nElem; i += kTileThreads) {
         const ushort4 lc = i == i0 ? lc0 : i == i1 ? lc1 : P.lconn[T.elemBegin + i];
         ElemCoords C;
         C.h0 = Xh[lc.x]; C.h1 = Xh[lc.y]; C.h2 = Xh[lc.z]; C.h3 = Xh[lc.w];
         C.l0 = Xl[lc.x]; C.l1 = Xl[lc.y]; C.l2 = Xl[lc.z]; C.l3 = Xl[lc.w];
         float g[12];
-        if (grad32_core(C, qthr2, g)) {
-            const int *nb = P.nodes + T.nodeBegin;
-            grad32_fp64(M.coord, make_int4(nb[lc.x], nb[lc.y], nb[lc.z], nb[lc.w]), g);
-            flagged++;
-        }
+        // a flagged element's slots are overwritten by the second pass
+        if (grad32_core(C, qthr2, g)) sFlag[atomicAdd(&sFlagged, 1)] = (unsigned short)i;
 #pragma unroll
         for (int j = 0; j < 4; j++) G[gslot(i, j)] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
     }
-    if (flagged) atomicAdd(counters + 1, flagged);
     __syncthreads();
+    const int nFlagged = sFlagged;
+    if (nFlagged) {
+        const int *nb = P.nodes + T.nodeBegin;
+        for (int k = tid; k < nFlagged; k += kTileThreads) {
+            const int i = sFlag[k];
+            const ushort4 lc = P.lconn[T.elemBegin + i];
+            float g[12];
+            grad32_fp64(M.coord, make_int4(nb[lc.x], nb[lc.y], nb[lc.z], nb[lc.w]), g);
+#pragma unroll
+            for (int j = 0; j < 4; j++) G[gslot(i, j)] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
+        }
+        if (tid == 0) atomicAdd(counters + 1, nFlagged);
+        __syncthreads();
+    }
 
     // the contribution lists (barrier 1), over the node coordinates: the
     // generic-proxy reads above are ordered before the async-proxy writes

@@ -114,7 +114,8 @@ SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRow
     L.off = L.contrib + round_up(std::max(maxContribPad * 2, maxNodes * 32), 16);
     L.diag = L.off + maxOffPad * 16;
     L.res = L.diag + maxRowsPad * 8;
-    L.bar = L.res + round_up(maxRowsPad * 4 * kResStride, 16);
+    // row results (phase 3a on); before that the queue of flagged elements
+    L.bar = L.res + round_up(std::max(maxRowsPad * 4 * kResStride, maxElem * 2), 16);
     L.bytes = L.bar + 16;                               // two mbarriers
     return L;
 }
