@@ -318,6 +318,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar + 1);
     }
     // bounded wait for the staged segments (the CTA agrees on the outcome)
+    if (tid == 0) sNext = 0;   // phase 2's unit counter, set 0
     bool ok = false;
     for (unsigned it = 0; it < ctl.waitLimit && !ok; it++)
         ok = mbar_try_wait(bar, 0) && mbar_try_wait(bar + 1, 0);
@@ -338,14 +339,19 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
             __syncthreads();
             const float2 *w = S.w + (size_t)set * S.wStride;
             for (int i = tid; i < T.nElem; i += kTileThreads) W[i] = w[P.elems[T.elemBegin + i]];
+            if (tid == 0) sNext = 0;
             __syncthreads();
         }
 
         // 3a. diagonal entries: four lanes per row sum a quarter of the row's
         //     contributions each and combine them without error; the first lane
-        //     writes the block and keeps the compensated sums for 3b
+        //     writes the block and keeps the compensated sums for 3b.  Only the
+        //     warps these lanes need take part; the others go straight to phase
+        //     2, which does not depend on 3a.
+        const int diagThreads = min(kTileThreads, (T.nRows * 4 + 31) & ~31);
+        if (tid < diagThreads) {
         const int part = tid & 3;
-        for (int base = 0; base < T.nRows; base += kTileThreads / 4) {
+        for (int base = 0; base < T.nRows; base += diagThreads / 4) {
             const int rl = base + (tid >> 2);
             const bool active = rl < T.nRows;
             const int2 de = active ? sDiag[rl] : make_int2(0, 0);
@@ -397,13 +403,13 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 }
             }
         }
-        if (tid == 0) sNext = 0;
-        __syncthreads();   // row sums of 3a and the unit counter are ready
+        // the row sums of 3a are ready for the diagonal warps (named barrier 1)
+        asm volatile("bar.sync 1, %0;" ::"r"(diagThreads) : "memory");
         if (PREC) {
             // 3b. one thread per row (full warps on the FP64 pipe): the FP64
             //     preconditioner block from the compensated sums, while the
-            //     other warps start on phase 2
-            for (int rl = tid; rl < T.nRows; rl += kTileThreads) {
+            //     other warps work on phase 2
+            for (int rl = tid; rl < T.nRows; rl += diagThreads) {
                 const int r = sDiag[rl].x;
                 const float *res = sRes + kResStride * rl;
                 if (OP == MFEM_OP_LAP) {
@@ -426,6 +432,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 }
             }
         }
+        }   // diagonal warps
 
         // 2. off-diagonal units: entry (r, c) and, when c is a row of this tile,
         //    its transpose (c, r), which is the same sum transposed; warps take
