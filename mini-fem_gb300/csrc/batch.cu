@@ -70,7 +70,7 @@ namespace mfem {
 namespace {
 
 template <bool PREC>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, 4)
 k_batch_tile32(const BatchMesh *__restrict__ meshes, const TileDesc *__restrict__ desc,
                const int *__restrict__ order, int nWork, SmemLayout L, float qthr2, int *counters,
                int *workCounter, TileCtl ctl) {
@@ -101,7 +101,7 @@ void prepare(mfem_batch &b) {
     MFEM_REQUIRE(!b.items.empty(), MFEM_ERR_STATE, "empty batch");
     // sizes and offsets
     b.totalVal = b.totalPrec = b.totalNodes = 0;
-    int maxW = 0, maxWW = 0, maxC = 0, maxO = 0, maxD = 0, maxR = 0;
+    int pm[5] = {1, 0, 0, 0, 0};   // plan maxima over the meshes (smem_layout's arguments)
     std::vector<TileDesc> all;
     std::vector<long long> cost;
     size_t maxRec = 0;
@@ -119,13 +119,7 @@ void prepare(mfem_batch &b) {
         b.totalPrec += (size_t)c.nbNodes * op_dim(it->op) * it->nSets;
         b.totalNodes += (size_t)c.nbNodes;
         maxRec = std::max(maxRec, (size_t)c.nbElem * 16);
-        const SmemLayout &L = c.tiles.layout;
-        maxW = std::max(maxW, L.w);
-        maxWW = std::max(maxWW, L.contrib - L.w);
-        maxC = std::max(maxC, L.off - L.contrib);
-        maxO = std::max(maxO, L.diag - L.off);
-        maxD = std::max(maxD, L.res - L.diag);
-        maxR = std::max(maxR, L.bar - L.res);
+        for (int k = 0; k < 5; k++) pm[k] = std::max(pm[k], c.tiles.planMax[k]);
         std::vector<TileDesc> d(c.tiles.nTiles);
         MFEM_CUDA(cudaMemcpy(d.data(), c.tiles.desc.ptr, sizeof(TileDesc) * d.size(), cudaMemcpyDeviceToHost));
         for (auto &t : d) {
@@ -134,15 +128,8 @@ void prepare(mfem_batch &b) {
             cost.push_back((long long)t.nElem * 4 + (long long)t.nContrib * it->nSets);
         }
     }
-    // shared-memory layout holding any tile of any mesh: region-wise maxima
-    SmemLayout L;
-    L.w = maxW;
-    L.contrib = L.w + maxWW;
-    L.off = L.contrib + maxC;
-    L.diag = L.off + maxO;
-    L.res = L.diag + maxD;
-    L.bar = L.res + maxR;
-    L.bytes = L.bar + 16;
+    // shared-memory layout holding any tile of any mesh
+    const SmemLayout L = smem_layout(pm[0], pm[1], pm[2], pm[3], pm[4]);
     b.layout = L;
     MFEM_REQUIRE(L.bytes <= 227 * 1024, MFEM_ERR_CAPACITY, "batch: tiles need more than 227 KB");
     // work list

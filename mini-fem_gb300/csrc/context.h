@@ -39,6 +39,7 @@ struct TilePlan {
     long long nUnits = 0;       // off-diagonal units (an intra-tile pair counts once)
     long long nContrib = 0;     // contributions summed per coefficient set
     SmemLayout layout{};
+    int planMax[5] = {1, 0, 0, 0, 0};   // largest tile: elements, contributions, off entries, rows, nodes
     DevBuf desc, elems, lconn, nodes, offEnt, diagEnt, contrib;
     DevBuf w32;                 // per-element weights of the current coefficients
 };

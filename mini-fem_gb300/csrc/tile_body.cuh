@@ -236,24 +236,25 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     __shared__ int sFlagged;   // elements of phase 1b queued for the FP64 gradients
     if (tid == 0) sFlagged = 0;
 
-    // 0. stage the entry tables with the TMA engine (barrier 0)
+    // 0. stage the contribution lists and the diagonal table with the TMA
+    //    engine (barrier 0)
     if (tid == 0) {
         mbar_init(bar, 1);
         mbar_init(bar + 1, 1);
         // make the initialised barriers visible to the TMA (async) proxy
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const unsigned bo = (unsigned)T.nOffPad * 16u, bd = (unsigned)T.nRowsPad * 8u;
-        mbar_expect_tx(bar, bo + bd + ctl.extraTx);
-        if (bo) bulk_g2s(sOff, P.offEnt + T.offBegin, bo, bar);
+        const unsigned bc = (unsigned)T.nContribPad * 2u, bd = (unsigned)T.nRowsPad * 8u;
+        mbar_expect_tx(bar, bc + bd + ctl.extraTx);
+        if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar);
         if (bd) bulk_g2s(sDiag, P.diagEnt + T.diagBegin, bd, bar);
     }
 
     // 1a. the weights of set 0 go to shared memory by asynchronous copies
     //     (cp.async, no register round trip); the connectivity of a thread's
     //     first two elements is loaded into registers; meanwhile the tile's node
-    //     coordinates (hi and lo parts) are gathered into the contribution
-    //     region, which the contribution lists fill only after phase 1
+    //     coordinates (hi parts, then lo parts) are gathered into the region
+    //     that the off-diagonal table fills after phase 1
     const int i0 = tid, i1 = tid + kTileThreads;
     ushort4 lc0 = make_ushort4(0, 0, 0, 0), lc1 = lc0;
     if (i0 < T.nElem) {
@@ -266,7 +267,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     }
     for (int i = i1 + kTileThreads; i < T.nElem; i += kTileThreads)
         cp_async8(W + i, S.w + P.elems[T.elemBegin + i]);
-    float4 *Xh = reinterpret_cast<float4 *>(sm + L.contrib);
+    float4 *Xh = reinterpret_cast<float4 *>(sm + L.x);
     float4 *Xl = Xh + T.nNodes;
     for (int i = tid; i < T.nNodes; i += kTileThreads) {
         const int n = P.nodes[T.nodeBegin + i];
@@ -276,12 +277,11 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     cp_async_wait_all();
     __syncthreads();
 
-    // 1b. gradients of the tile's elements; flagged elements are queued (in
-    //     the row-result region, unused until phase 3a) and get their FP64
-    //     gradients in a second pass by consecutive threads, so that the FP64
-    //     work is spread over full warps instead of stalling every warp that
-    //     holds one flagged element
-    unsigned short *sFlag = reinterpret_cast<unsigned short *>(sm + L.res);
+    // 1b. gradients of the tile's elements; flagged elements are queued (after
+    //     the coordinates) and get their FP64 gradients in a second pass by
+    //     consecutive threads, so that the FP64 work is spread over full warps
+    //     instead of stalling every warp that holds one flagged element
+    unsigned short *sFlag = reinterpret_cast<unsigned short *>(sm + L.q);
     for (int i = tid; i < T.nElem; i += kTileThreads) {
         const ushort4 lc = i == i0 ? lc0 : i == i1 ? lc1 : P.lconn[T.elemBegin + i];
         ElemCoords C;
@@ -309,27 +309,30 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         __syncthreads();
     }
 
-    // the contribution lists (barrier 1), over the node coordinates: the
-    // generic-proxy reads above are ordered before the async-proxy writes
+    // the off-diagonal table (barrier 1), over the node coordinates: the
+    // generic-proxy reads above are ordered before the async-proxy writes.
+    // Only phase 2 reads it; each warp waits for it just before its phase 2.
     if (tid == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const unsigned bc = (unsigned)T.nContribPad * 2u;
-        mbar_expect_tx(bar + 1, bc);
-        if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar + 1);
+        const unsigned bo = (unsigned)T.nOffPad * 16u;
+        mbar_expect_tx(bar + 1, bo);
+        if (bo) bulk_g2s(sOff, P.offEnt + T.offBegin, bo, bar + 1);
     }
-    // bounded wait for the staged segments (the CTA agrees on the outcome)
+    // bounded wait for the contribution lists and the diagonal table (the CTA
+    // agrees on the outcome)
     if (tid == 0) sNext = 0;   // phase 2's unit counter, set 0
     bool ok = false;
-    for (unsigned it = 0; it < ctl.waitLimit && !ok; it++)
-        ok = mbar_try_wait(bar, 0) && mbar_try_wait(bar + 1, 0);
+    for (unsigned it = 0; it < ctl.waitLimit && !ok; it++) ok = mbar_try_wait(bar, 0);
     if (__syncthreads_or(!ok)) {
-        if (tid == 0) atomicOr(counters + 2, 1);
+        if (tid == 0) {
+            atomicOr(counters + 2, 1);
+            // let the off-diagonal copy land (bounded) before the CTA exits
+            for (unsigned it = 0; it < ctl.waitLimit && !mbar_try_wait(bar + 1, 0); it++) {
+            }
+        }
         return false;
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar + 1)) : "memory");
-    }
+    bool offMissing = false;   // this warp gave up waiting for the off-diagonal table
 
     for (int set = 0; set < S.nSets; set++) {
         float *values = S.values + (size_t)set * S.valuesStride;
@@ -436,9 +439,15 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
 
         // 2. off-diagonal units: entry (r, c) and, when c is a row of this tile,
         //    its transpose (c, r), which is the same sum transposed; warps take
-        //    32 units at a time from a shared counter, so that the warps of 3b
-        //    join when their FP64 work is done
-        for (;;) {
+        //    32 units at a time from a shared counter, so that the warps of 3a
+        //    and 3b join when their work is done.  First a bounded wait (warp-
+        //    uniform outcome) for the off-diagonal table.
+        if (set == 0) {
+            bool got = false;
+            for (unsigned it = 0; it < ctl.waitLimit && !got; it++) got = mbar_try_wait(bar + 1, 0);
+            offMissing = !__all_sync(0xffffffffu, got);
+        }
+        for (; !offMissing;) {
             int base = 0;
             if (lane == 0) base = atomicAdd(&sNext, 32);
             base = __shfl_sync(0xffffffffu, base, 0);
@@ -488,6 +497,14 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 }
             }
         }
+    }
+    if (__syncthreads_or(offMissing)) {
+        if (tid == 0) atomicOr(counters + 2, 1);
+        return false;
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar + 1)) : "memory");
     }
     return true;
 }

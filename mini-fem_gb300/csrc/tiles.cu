@@ -39,7 +39,7 @@ namespace mfem {
 namespace {
 
 template <int OP, bool PREC>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, 4)
 k_tile32(TilePlanView P, TileMesh M, TileSets S, SmemLayout L, float qthr2, int *counters,
          TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -111,11 +111,13 @@ SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRow
     SmemLayout L;
     L.w = maxElem * 64;                                 // gradients: 4 float4 per element
     L.contrib = L.w + round_up(maxElem * 8, 16);        // weights: float2 per element
-    L.off = L.contrib + round_up(std::max(maxContribPad * 2, maxNodes * 32), 16);
-    L.diag = L.off + maxOffPad * 16;
-    L.res = L.diag + maxRowsPad * 8;
-    // row results (phase 3a on); before that the queue of flagged elements
-    L.bar = L.res + round_up(std::max(maxRowsPad * 4 * kResStride, maxElem * 2), 16);
+    L.diag = L.contrib + round_up(maxContribPad * 2, 16);
+    L.off = L.diag + maxRowsPad * 8;                    // after phase 1: off-diagonal table,
+    L.res = L.off + maxOffPad * 16;                     //   then the row results
+    L.x = L.off;                                        // during phase 1: coordinates,
+    L.q = L.x + maxNodes * 32;                          //   then the flagged-element queue
+    const int lateEnd = std::max(L.res + maxRowsPad * 4 * kResStride, L.q + maxElem * 2);
+    L.bar = round_up(lateEnd, 16);
     L.bytes = L.bar + 16;                               // two mbarriers
     return L;
 }
@@ -334,6 +336,11 @@ void build_tile_plan_impl(Context &c) {
 
     tp.nTiles = (int)tiles.size();
     tp.layout = smem_layout(std::max(maxElem, 1), maxContrib, maxOff, maxRows, maxNodes);
+    tp.planMax[0] = std::max(maxElem, 1);
+    tp.planMax[1] = maxContrib;
+    tp.planMax[2] = maxOff;
+    tp.planMax[3] = maxRows;
+    tp.planMax[4] = maxNodes;
     MFEM_REQUIRE(tp.layout.bytes <= 227 * 1024, MFEM_ERR_CAPACITY,
                  "tile plan: a tile needs more than 227 KB of shared memory");
     auto up = [&](DevBuf &d, const void *src, size_t bytes) {

@@ -67,11 +67,12 @@ struct TileCtl {
     unsigned extraTx;
 };
 
-// Byte offsets of the dynamic shared-memory regions.  The contribution region
-// holds the tile's node coordinates (32 bytes per node) while the gradients are
-// computed, then the contribution lists.
+// Byte offsets of the dynamic shared-memory regions.  The tile's node
+// coordinates (x: hi parts, then lo parts, 32 bytes per node) and the queue of
+// flagged elements (q) are needed only during phase 1; they share a region with
+// the off-diagonal table and the row results, which are filled after it.
 struct SmemLayout {
-    int w, contrib, off, diag, res, bar, bytes;
+    int w, contrib, diag, off, res, x, q, bar, bytes;
 };
 
 SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes);
