@@ -22,10 +22,12 @@ __global__ void k_split_coords(const double *__restrict__ coord, int nbNodes,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbNodes) return;
     const double x = coord[3 * i], y = coord[3 * i + 1], z = coord[3 * i + 2];
-    const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
+    float xh, yh, zh, xl, yl, zl;
+    split_hilo(x, xh, xl);
+    split_hilo(y, yh, yl);
+    split_hilo(z, zh, zl);
     hi[i] = make_float4(xh, yh, zh, 0.f);
-    lo[i] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
-                        __double2float_rn(z - (double)zh), 0.f);
+    lo[i] = make_float4(xl, yl, zl, 0.f);
 }
 
 // FP32 coefficients of the record kernel: kappa (lap) or (E, 1/2 - nu) (ela,

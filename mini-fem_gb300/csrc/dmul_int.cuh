@@ -26,6 +26,7 @@
 #pragma once
 
 #include <stdint.h>
+#include <string.h>
 
 #ifdef __CUDACC__
 #define MFEM_HD __host__ __device__ __forceinline__
@@ -57,6 +58,39 @@ MFEM_HD bool dmul_bits(uint64_t A, uint64_t B, uint64_t *out) {
     const uint64_t r = (m + ((1ull << (sh - 1u)) - 1ull) + ((m >> sh) & 1ull)) >> sh;
     *out = ((((uint64_t)(uint32_t)(e + (int)top)) << 52) + r) |
            ((uint64_t)((ah ^ bh) & 0x80000000u) << 32);
+    return true;
+}
+
+// hi = fl32(x) and lo = fl32(x - hi) (round to nearest even; x - hi is exact in
+// FP64) from the bit pattern X of a double with biased exponent in
+// [1023 - 60, 1023 + 100]; returns false otherwise (zero, tiny, huge, special).
+// The dropped 29 significand bits give x - hi directly: m29 when hi was
+// rounded down, -(2^29 - m29) when it was rounded up, times 2^(e - 1075); the
+// FP32 rounding of that integer is a u32 -> f32 conversion and an exponent add.
+MFEM_HD bool split_f32_bits(uint64_t X, uint32_t *hi, uint32_t *lo) {
+    const uint32_t hw = (uint32_t)(X >> 32), lw = (uint32_t)X;
+    const uint32_t e = (hw >> 20) & 0x7ffu;
+    if (e < 1023u - 60u || e > 1023u + 100u) return false;
+    const uint32_t sign = hw & 0x80000000u;
+    const uint32_t m23 = ((hw & 0xfffffu) << 3) | (lw >> 29);
+    const uint32_t m29 = lw & 0x1fffffffu;
+    const bool up = m29 > 0x10000000u || (m29 == 0x10000000u && (m23 & 1u));
+    *hi = (sign | ((e - 1023u + 127u) << 23) | m23) + (up ? 1u : 0u);
+    const uint32_t mag = up ? 0x20000000u - m29 : m29;
+    if (mag == 0u) {
+        *lo = 0u;
+        return true;
+    }
+#ifdef __CUDA_ARCH__
+    const float f = __uint2float_rn(mag);
+    uint32_t fb = __float_as_uint(f);
+#else
+    const float f = (float)mag;
+    uint32_t fb;
+    memcpy(&fb, &f, 4);
+#endif
+    fb += (uint32_t)((int32_t)e - 1075) << 23;
+    *lo = fb | (up ? sign ^ 0x80000000u : sign);
     return true;
 }
 

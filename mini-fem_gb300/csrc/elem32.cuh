@@ -113,13 +113,16 @@ __device__ __forceinline__ double f32_to_f64(float x) {
 
 // Weights of the FP32 blocks: (B, mu) for ela, (kappa, 0) for lap, from the FP64
 // per-element coefficients (NULL: the reference constants B = 1.25, mu = 1,
-// kappa = 1).  One FP64 subtraction per element (1/2 - nu).
+// kappa = 1).  1/2 - nu from the hi/lo split of nu, within an FP32 ulp, without
+// the FP64 pipe.
 template <int OP>
 __device__ __forceinline__ float2 weights32(const double *__restrict__ coef, int e) {
     if (OP == MFEM_OP_LAP) return make_float2(coef ? f64_to_f32(coef[e]) : 1.0f, 0.f);
     if (!coef) return make_float2(1.25f, 1.0f);
     const double2 c = reinterpret_cast<const double2 *>(coef)[e];
-    return lame32(f64_to_f32(c.x), f64_to_f32(0.5 - c.y));
+    float nh, nl;
+    split_hilo(c.y, nh, nl);
+    return lame32(f64_to_f32(c.x), (0.5f - nh) - nl);
 }
 
 struct Kahan {

@@ -153,6 +153,19 @@ __device__ __forceinline__ double lap_entry(const double *gj, const double *gk, 
     return REFW ? s : dmul<W>(kappa, s);
 }
 
+// hi + lo split of a coordinate: hi = fl32(x), lo = fl32(x - hi), on the
+// integer pipes (split_f32_bits) except for zero and extreme magnitudes.
+__device__ __forceinline__ void split_hilo(double x, float &h, float &l) {
+    uint32_t hb, lb;
+    if (split_f32_bits((uint64_t)__double_as_longlong(x), &hb, &lb)) {
+        h = __uint_as_float(hb);
+        l = __uint_as_float(lb);
+    } else {
+        h = __double2float_rn(x);
+        l = __double2float_rn(x - (double)h);
+    }
+}
+
 // Lame weights (B, mu) = (lambda + mu, mu) in FP32 from Young's modulus E and
 // h = 1/2 - nu, rounded to FP32 from its FP64 value: then 1 - 2 nu = 2h, 1 + nu =
 // 3/2 - h and nu = 1/2 - h carry no cancellation, where 1 - 2 nu formed from an

@@ -61,10 +61,12 @@ __global__ void k_split_coords_t(const double *__restrict__ coord, int nbNodes,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbNodes) return;
     const double x = coord[3 * i], y = coord[3 * i + 1], z = coord[3 * i + 2];
-    const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
+    float xh, yh, zh, xl, yl, zl;
+    split_hilo(x, xh, xl);
+    split_hilo(y, yh, yl);
+    split_hilo(z, zh, zl);
     hl[2 * i] = make_float4(xh, yh, zh, 0.f);
-    hl[2 * i + 1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
-                                __double2float_rn(z - (double)zh), 0.f);
+    hl[2 * i + 1] = make_float4(xl, yl, zl, 0.f);
 }
 
 // The FP32 step's two inputs in one launch: threads [0, nbNodes) split one
@@ -77,10 +79,12 @@ __global__ void k_split_and_weights(const double *__restrict__ coord, int nbNode
     if (t < nbNodes) {
         const int i = (int)t;
         const double x = coord[3 * (size_t)i], y = coord[3 * (size_t)i + 1], z = coord[3 * (size_t)i + 2];
-        const float xh = __double2float_rn(x), yh = __double2float_rn(y), zh = __double2float_rn(z);
+        float xh, yh, zh, xl, yl, zl;
+        split_hilo(x, xh, xl);
+        split_hilo(y, yh, yl);
+        split_hilo(z, zh, zl);
         hl[2 * (size_t)i] = make_float4(xh, yh, zh, 0.f);
-        hl[2 * (size_t)i + 1] = make_float4(__double2float_rn(x - (double)xh), __double2float_rn(y - (double)yh),
-                                            __double2float_rn(z - (double)zh), 0.f);
+        hl[2 * (size_t)i + 1] = make_float4(xl, yl, zl, 0.f);
     } else if (t - nbNodes < nbElem) {
         w[t - nbNodes] = weights32<OP>(coef, (int)(t - nbNodes));
     }

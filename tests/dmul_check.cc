@@ -1,6 +1,7 @@
-// CPU check of the integer-pipe double multiplication (the header's portable
-// path) against the host's IEEE multiplication: random bit patterns, operands
-// near 1.0, short significands (ties), and exhaustive small-integer products.
+// CPU check of the integer-pipe double multiplication and hi/lo split (the
+// header's portable path) against the host's IEEE arithmetic: random bit
+// patterns, operands near 1.0, short significands (ties), exhaustive
+// small-integer products, and splits with ties in the dropped bits.
 // Usage: dmul_check <pairs> <seed>; prints "<fast> <mismatches>".
 #include <cstdio>
 #include <cstdlib>
@@ -56,6 +57,29 @@ int main(int argc, char **argv) {
     for (uint64_t x = 1; x < 2048; x++)
         for (uint64_t y = 1; y < 2048; y++)
             check(as_bits((double)x * 1.5), as_bits((double)(9007199254740992ull - y)));
+    // hi/lo split of doubles: fl32(x) and fl32(x - fl32(x)), random patterns
+    // with exponents around 1.0 and ties of the 29 dropped bits
+    for (long long i = 0; i < n; i++) {
+        uint64_t X = next();
+        X = (X & 0x800fffffffffffffull) | ((uint64_t)(963 + (X >> 40) % 161) << 52);
+        if (i % 4 == 1) X = (X & ~0x1fffffffull) | 0x10000000ull;        // exact tie
+        if (i % 4 == 2) X &= ~0x1fffffffull;                             // exact in FP32
+        uint32_t h, l;
+        if (!mfem::split_f32_bits(X, &h, &l)) continue;
+        fast++;
+        volatile double x = as_double(X);
+        const float rh = (float)x;
+        volatile double rest = x - (double)rh;
+        const float rl = (float)rest;
+        uint32_t bh, bl;
+        std::memcpy(&bh, &rh, 4);
+        std::memcpy(&bl, &rl, 4);
+        if (h != bh || l != bl) {
+            if (bad < 5) std::printf("# split %016llx: %08x %08x != %08x %08x\n",
+                                     (unsigned long long)X, h, l, bh, bl);
+            bad++;
+        }
+    }
     std::printf("%llu %llu\n", fast, bad);
     return bad != 0;
 }
