@@ -24,14 +24,6 @@ struct ElemCoords {
     float4 h0, h1, h2, h3, l0, l1, l2, l3;
 };
 
-__device__ __forceinline__ ElemCoords load_coords(const float4 *__restrict__ hi,
-                                                  const float4 *__restrict__ lo, int4 nd) {
-    ElemCoords c;
-    c.h0 = hi[nd.x]; c.h1 = hi[nd.y]; c.h2 = hi[nd.z]; c.h3 = hi[nd.w];
-    c.l0 = lo[nd.x]; c.l1 = lo[nd.y]; c.l2 = lo[nd.z]; c.l3 = lo[nd.w];
-    return c;
-}
-
 // Gradients g[4][3] of one element in FP32 from its loaded coordinates.
 // Returns true, with g not computed, when the element is flagged: quality
 // |6V| / (|a||b||c|) below sqrt(qthr2).
@@ -68,21 +60,6 @@ __device__ __forceinline__ void grad32_fp64(const double *__restrict__ coord, in
     elem_gradients(coord, nd, gd);
 #pragma unroll
     for (int i = 0; i < 12; i++) g[i] = f64_to_f32(gd[i]);
-}
-
-// grad32_core, with flagged elements computed in FP64 from `coord`; returns
-// whether the element was flagged.
-__device__ __forceinline__ bool grad32_from(const ElemCoords &C, const double *__restrict__ coord,
-                                            int4 nd, float qthr2, float g[12]) {
-    if (!grad32_core(C, qthr2, g)) return false;
-    grad32_fp64(coord, nd, g);
-    return true;
-}
-
-__device__ __forceinline__ bool grad32(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
-                                       const double *__restrict__ coord, int4 nd, float qthr2,
-                                       float g[12]) {
-    return grad32_from(load_coords(hi, lo, nd), coord, nd, qthr2, g);
 }
 
 // double -> float, round to nearest even, with integer operations so that it
@@ -135,29 +112,5 @@ struct Kahan {
     }
     __device__ __forceinline__ float value() const { return s - c; }
 };
-
-// Inverse of a symmetric-positive 3x3 block (column-major, FP64) by cofactors
-// with FMAs; returns false when the determinant is exactly zero (block left as
-// it is).  Used by the FP32 path, whose preconditioner is not tied to the
-// reference's LAPACK operation order.
-__device__ __forceinline__ bool inv3_cofactor(double a[9]) {
-    const double c00 = fma(a[4], a[8], -a[7] * a[5]);
-    const double c01 = fma(a[7], a[2], -a[1] * a[8]);
-    const double c02 = fma(a[1], a[5], -a[4] * a[2]);
-    const double det = fma(a[0], c00, fma(a[3], c01, a[6] * c02));
-    if (det == 0.0) return false;
-    const double r = 1.0 / det;
-    const double c10 = fma(a[6], a[5], -a[3] * a[8]);
-    const double c11 = fma(a[0], a[8], -a[6] * a[2]);
-    const double c12 = fma(a[3], a[2], -a[0] * a[5]);
-    const double c20 = fma(a[3], a[7], -a[6] * a[4]);
-    const double c21 = fma(a[6], a[1], -a[0] * a[7]);
-    const double c22 = fma(a[0], a[4], -a[3] * a[1]);
-    // inverse(i,j) = cofactor(j,i) / det, column-major
-    a[0] = c00 * r; a[1] = c01 * r; a[2] = c02 * r;
-    a[3] = c10 * r; a[4] = c11 * r; a[5] = c12 * r;
-    a[6] = c20 * r; a[7] = c21 * r; a[8] = c22 * r;
-    return true;
-}
 
 }  // namespace mfem
