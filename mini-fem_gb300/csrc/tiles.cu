@@ -4,23 +4,27 @@
 // tiles of at most maxRows rows whose incident elements number at most maxElem.
 // One CTA per tile:
 //   0. one thread starts TMA bulk copies (cp.async.bulk, completion on an
-//      mbarrier) of the tile's off-diagonal entry table and diagonal table;
+//      mbarrier) of the tile's contribution lists and diagonal table;
 //   1. meanwhile the CTA gathers the coordinates of the tile's nodes (one
-//      32-byte sector per node) into shared memory, then computes the FP32
-//      gradients and weights of the elements incident to the tile's rows
-//      (ascending element id, connectivity as indices into the tile's node
-//      list) into shared memory: each element once per tile that needs it, no
-//      records in HBM; the contribution lists are then copied (second
-//      mbarrier) over the node coordinates, which are no longer needed;
+//      32-byte sector per node) into the shared-memory region that the
+//      off-diagonal table fills later, then computes the FP32 gradients of the
+//      elements incident to the tile's rows (ascending element id,
+//      connectivity as indices into the tile's node list) into shared memory:
+//      each element once per tile that needs it, no records in HBM; elements
+//      below the quality threshold are queued and get FP64 gradients in a
+//      second pass by consecutive threads; the off-diagonal table is then
+//      copied (second mbarrier) over the coordinates, and each warp waits for
+//      it only when it reaches phase 2;
 //   3a. four lanes per diagonal entry sum a quarter of its contributions each
 //      and combine them with error-free additions; the first of the four writes
-//      the block and keeps the compensated sums;
+//      the block and keeps the compensated sums.  Only the warps these lanes
+//      fill take part; the others start phase 2 at once;
 //   3b. one thread per row (the first warps) masks the block and inverts it in
-//      FP64 into the preconditioner, while the other warps already run phase 2;
+//      FP64 into the preconditioner, while the other warps run phase 2;
 //   2. one thread per off-diagonal entry sums its contributions with Kahan
 //      compensation and writes the 3x3 block (or scalar) to the CSR values;
 //      warps take 32 entries at a time from a shared counter, so that the warps
-//      of 3b join when their FP64 work is done.
+//      of 3a and 3b join when their work is done.
 // The plan is built once per mesh on the host from the device pattern.  Every
 // contribution list is in ascending element order and every combination order
 // is fixed, so results are deterministic.
