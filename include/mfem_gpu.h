@@ -80,6 +80,16 @@ int mfem_update_coords(mfem_context *ctx, const double *coord);
  * capacity < nnz (nothing written to col then). */
 int mfem_create_nodeToNode(mfem_context *ctx, int order, int *row, int *col,
                            int capacity, int *nbEdges);
+/* create_nodeToNode exactly as src/matrix.cc:55-91 computes it from the
+ * caller's node -> element lists (index_t nodeToElem of src/main.cc:243-247:
+ * index[nbNodes+1], value[index[nbNodes]] = 0-based element ids): the columns of
+ * row i are the distinct nodes of the elements value[index[i] .. index[i+1]) in
+ * first-occurrence order, walking the lists in the caller's order (the order
+ * DC-lib produced).  Other arguments as mfem_create_nodeToNode with
+ * MFEM_ORDER_REFERENCE. */
+int mfem_create_nodeToNode_incidence(mfem_context *ctx, const int *nodeToElemIndex,
+                                     const int *nodeToElemValue, int *row, int *col,
+                                     int capacity, int *nbEdges);
 /* elemToEdge[nbElem*16]: 0-based CSR position of (j,k), j-major. */
 int mfem_create_elemToEdge(mfem_context *ctx, int *elemToEdge);
 /* Adopts a pattern the caller built (row 0-based, col 1-based, any column order).
@@ -218,9 +228,10 @@ int mfem_pcg(mfem_context *ctx, const double *b, double *x, double rtol, int max
 
 /* ---- allocation-free assembly ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory while they assemble -- code recorded into a CUDA graph by stream
- * capture, solvers whose device memory belongs to their own pool allocator,
- * real-time loops that must not risk an allocation failure -- this runs the
+ * memory while they assemble -- solvers whose device memory belongs to their
+ * own pool allocator, time-stepping loops that must not stall on cudaFree's
+ * implicit device synchronisation, real-time loops that must not risk an
+ * allocation failure -- this runs the
  * FP64 gather (the kernels and results of mfem_assemble with MFEM_FP64 and
  * MFEM_GATHER, without the preconditioner) and calls no cudaMalloc, cudaFree or
  * allocating library routine.  coord (nbNodes*3), coef (as
@@ -234,7 +245,13 @@ int mfem_pcg(mfem_context *ctx, const double *b, double *x, double rtol, int max
  * it), so make that first call before any stream capture.  Work is enqueued on
  * `stream` (a cudaStream_t, NULL for the legacy default stream) without waiting.
  * All calls share the one array and every call overwrites it: calls that overlap
- * on the GPU (e.g. on two streams) race and must be serialised by the caller. */
+ * on the GPU (e.g. on two streams) race and must be serialised by the caller.
+ * The kernels also read the context's topology and gather plan on `stream`,
+ * which is not ordered with the context's own stream: drain `stream` (or make
+ * the context stream wait for it) before mfem_set_mesh, mfem_create_nodeToNode,
+ * mfem_set_pattern or mfem_destroy change or free them.  The calling thread's
+ * current device is left as it was; `stream` must belong to the context's
+ * device (MFEM_ERR_INVALID_ARG otherwise). */
 int mfem_assemble_noalloc(mfem_context *ctx, int operatorID, const double *coord,
                           const double *coef, double *values, void *stream);
 

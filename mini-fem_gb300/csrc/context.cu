@@ -89,6 +89,35 @@ void require_pattern(Context &c) {
     MFEM_REQUIRE(c.hasPattern, MFEM_ERR_STATE, "no CSR pattern (create_nodeToNode first)");
 }
 
+// Order-dependent 64-bit fingerprint of n int32 values (four independent
+// multiply-xorshift chains over 8-byte words, then folded): any change of the
+// contents, a permutation of the element rows included, changes it with
+// overwhelming probability.  Cost at 5.8M elements: a few ms on one core,
+// against the 1 GB copy-out of the values that the same call makes.
+unsigned long long fingerprint_i32(const int *a, long long n) {
+    const unsigned long long K = 0x9E3779B97F4A7C15ULL;
+    unsigned long long h[4] = {0x243F6A8885A308D3ULL, 0x13198A2E03707344ULL,
+                               0xA4093822299F31D0ULL, 0x082EFA98EC4E6C89ULL};
+    long long i = 0;
+    for (; i + 8 <= n; i += 8)
+        for (int l = 0; l < 4; l++) {
+            unsigned long long w;
+            std::memcpy(&w, a + i + 2 * l, sizeof(w));
+            h[l] = (h[l] ^ w) * K;
+            h[l] ^= h[l] >> 29;
+        }
+    for (; i < n; i++) {
+        h[0] = (h[0] ^ (unsigned)a[i]) * K;
+        h[0] ^= h[0] >> 29;
+    }
+    unsigned long long r = (unsigned long long)n;
+    for (int l = 0; l < 4; l++) {
+        r = (r ^ h[l]) * K;
+        r ^= r >> 31;
+    }
+    return r;
+}
+
 void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int nbNodes) {
     MFEM_REQUIRE(e2n, MFEM_ERR_INVALID_ARG, "null elemToNode");
     MFEM_REQUIRE(nbElem > 0 && nbNodes > 0, MFEM_ERR_INVALID_ARG, "empty mesh");
@@ -124,6 +153,7 @@ void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int n
         throw Error(MFEM_ERR_INVALID_ARG, "elemToNode holds a node outside [1, nbNodes]");
     }
     c.hostE2n = e2n;
+    c.hostE2nSig = fingerprint_i32(e2n, n4);
 }
 
 // Errors kernels report through the status words after they were enqueued:
@@ -374,6 +404,26 @@ int mfem_create_nodeToNode(mfem_context *ctx, int order, int *row, int *col, int
     return mfem::guarded(ctx, [&](Context &c) {
         mfem::require_mesh(c);
         mfem::build_pattern(c, order);
+        if (nbEdges) *nbEdges = c.nnz;
+        if (row)
+            MFEM_CUDA(cudaMemcpyAsync(row, c.rowPtr.as<int>(), sizeof(int) * (c.nbNodes + 1),
+                                      cudaMemcpyDeviceToHost, c.stream));
+        if (col) {
+            MFEM_REQUIRE(capacity >= c.nnz, MFEM_ERR_CAPACITY, "column buffer smaller than nnz");
+            mfem::download_col(c, col);
+        }
+        MFEM_CUDA(cudaStreamSynchronize(c.stream));
+        c.hostRow = row;
+        c.hostCol = col;
+    });
+}
+
+int mfem_create_nodeToNode_incidence(mfem_context *ctx, const int *nodeToElemIndex,
+                                     const int *nodeToElemValue, int *row, int *col,
+                                     int capacity, int *nbEdges) {
+    return mfem::guarded(ctx, [&](Context &c) {
+        mfem::require_mesh(c);
+        mfem::build_pattern_from_incidence(c, nodeToElemIndex, nodeToElemValue);
         if (nbEdges) *nbEdges = c.nnz;
         if (row)
             MFEM_CUDA(cudaMemcpyAsync(row, c.rowPtr.as<int>(), sizeof(int) * (c.nbNodes + 1),
@@ -646,7 +696,11 @@ int mfem_assembly(mfem_context *ctx, double *coord, double *nodeToNodeValue, int
                      "operatorDim does not match operatorID");
         MFEM_REQUIRE(coord && nodeToNodeValue && nodeToNodeRow && nodeToNodeColumn && elemToNode,
                      MFEM_ERR_INVALID_ARG, "null argument");
-        if (c.nbElem != nbElem || c.hostE2n != elemToNode) {
+        // the mesh is re-uploaded (and the pattern re-adopted) when elemToNode is
+        // another array or the same array with other contents -- e.g. permuted
+        // in place as src/main.cc:229 does after coloring_creation
+        if (c.nbElem != nbElem || c.hostE2n != elemToNode ||
+            c.hostE2nSig != mfem::fingerprint_i32(elemToNode, 4LL * nbElem)) {
             int nbNodes = 0;
             for (long long i = 0; i < 4LL * nbElem; i++) nbNodes = std::max(nbNodes, elemToNode[i]);
             mfem::set_mesh(c, coord, elemToNode, nbElem, nbNodes);

@@ -107,6 +107,7 @@ struct Context {
     DevBuf coord;      // double [N*3]
     DevBuf e2n;        // int    [E*4], 0-based
     const void *hostE2n = nullptr;   // identity of the caller's elemToNode
+    unsigned long long hostE2nSig = 0;   // and a fingerprint of its contents
 
     // pattern
     bool hasPattern = false;
@@ -161,6 +162,7 @@ struct Context {
 // pattern.cu
 void build_incidence(Context &c);
 void build_pattern(Context &c, int order);
+void build_pattern_from_incidence(Context &c, const int *hIndex, const int *hValue);
 void adopt_pattern(Context &c, const int *hRow, const int *hCol, int nnz);
 void build_elem_pos(Context &c);
 void build_gather_plan(Context &c);

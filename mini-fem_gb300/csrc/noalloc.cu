@@ -1,10 +1,10 @@
 // Allocation-free FP64 assembly (mfem_assemble_noalloc).
 //
-// Some callers cannot call cudaMalloc while they assemble: code recorded into a
-// CUDA graph by stream capture (allocation is not a capturable operation),
-// solvers whose device memory is owned by their own pool allocator and that
-// forbid other allocations after start-up, and real-time loops that must not
-// take the allocator's locks or risk an out-of-memory failure mid-run.  This
+// Some callers cannot call cudaMalloc while they assemble: solvers whose device
+// memory is owned by their own pool allocator and that forbid other allocations
+// after start-up, time-stepping loops that must not stall on cudaFree's implicit
+// device synchronisation, and real-time loops that must not take the
+// allocator's locks or risk an out-of-memory failure mid-run.  This
 // entry point runs the FP64 gather -- the same kernels as mfem_assemble with
 // MFEM_FP64 / MFEM_GATHER -- on buffers the caller passes (coordinates,
 // coefficients, values) and keeps its only scratch, the per-element gradient
@@ -35,11 +35,28 @@ std::mutex g_mutex;
 constexpr int kMaxDevices = 64;
 double *g_rec_addr[kMaxDevices] = {};
 
+// Makes `device` current for the scope and gives the caller's current device
+// back on every exit path, so the entry point leaves the calling thread's
+// device setting as it found it.
+struct DeviceScope {
+    int saved = -1;
+    explicit DeviceScope(int device) {
+        MFEM_CUDA(cudaGetDevice(&saved));
+        if (saved != device) MFEM_CUDA(cudaSetDevice(device));
+    }
+    ~DeviceScope() {
+        int now = -1;
+        if (saved >= 0 && cudaGetDevice(&now) == cudaSuccess && now != saved) cudaSetDevice(saved);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
+// Called with `device` current (DeviceScope).
 double *scratch_address(int device) {
     MFEM_REQUIRE(device >= 0 && device < kMaxDevices, MFEM_ERR_INVALID_ARG, "device id out of range");
     std::lock_guard<std::mutex> lock(g_mutex);
     if (!g_rec_addr[device]) {
-        MFEM_CUDA(cudaSetDevice(device));
         void *p = nullptr;
         const cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_rec);
         if (rc != cudaSuccess)
@@ -64,7 +81,13 @@ extern "C" int mfem_assemble_noalloc(mfem_context *ctx, int operatorID, const do
                      "no gather plan: call mfem_assemble(FP64, GATHER) once first");
         MFEM_REQUIRE(c.nbElem <= kNoAllocMaxElem, MFEM_ERR_CAPACITY,
                      "mesh larger than the 131072 elements of the allocation-free scratch");
-        MFEM_CUDA(cudaSetDevice(c.device));
+        DeviceScope scope(c.device);
+        if (stream) {
+            int sdev = -1;
+            MFEM_CUDA(cudaStreamGetDevice((cudaStream_t)stream, &sdev));
+            MFEM_REQUIRE(sdev == c.device, MFEM_ERR_INVALID_ARG,
+                         "stream belongs to another device than the context");
+        }
         double *rec = scratch_address(c.device);
         mfem::gather_fp64_into(c, operatorID, coord, coef, rec, values, (cudaStream_t)stream);
         c.lastError.clear();

@@ -398,16 +398,32 @@ void build_incidence(Context &c) {
     c.hasIncidence = true;
 }
 
-void build_pattern(Context &c, int order) {
-    MFEM_REQUIRE(order == MFEM_ORDER_SORTED || order == MFEM_ORDER_REFERENCE,
-                 MFEM_ERR_INVALID_ARG, "unknown column order");
-    build_incidence(c);
+namespace {
+
+// Caller's node -> element lists (0-based element ids) -> the e*4 form the row
+// kernels read (they use the element id only); ids outside [0, nbElem) are
+// flagged and replaced by 0.
+__global__ void k_caller_incidence(const int *__restrict__ in, int *__restrict__ out, long long n,
+                                   int nbElem, int *status) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int e = in[i];
+    if (e < 0 || e >= nbElem) {
+        atomicOr(status, kBadIndex);
+        e = 0;
+    }
+    out[i] = e << 2;
+}
+
+// Rows of the pattern from node -> element lists ptr/ne (any order within a
+// node; the first-occurrence column order follows it).
+void build_rows(Context &c, int order, const int *ptr, const int *ne) {
     const int N = c.nbNodes;
     int *st = status_ptr(c);
     MFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(int), c.stream));
     int *rowPtr = (int *)c.rowPtr.reserve(sizeof(int) * (N + 1));
     int *tmp = (int *)c.scanTmp.reserve(sizeof(int) * scan_tmp_elems(N + 1));
-    const int *ptr = c.nodeElemPtr.as<int>(), *ne = c.nodeElem.as<int>(), *e2n = c.e2n.as<int>();
+    const int *e2n = c.e2n.as<int>();
     int *longRows = (int *)c.scratch2.reserve(sizeof(int) * ((size_t)N + 1));
     int *nLongDev = longRows + N;
     MFEM_CUDA(cudaMemsetAsync(nLongDev, 0, sizeof(int), c.stream));
@@ -471,6 +487,49 @@ void build_pattern(Context &c, int order) {
     c.hasElemPos = false;
     c.gather.built = false;
     c.tiles.built = false;
+}
+
+}  // namespace
+
+void build_pattern(Context &c, int order) {
+    MFEM_REQUIRE(order == MFEM_ORDER_SORTED || order == MFEM_ORDER_REFERENCE,
+                 MFEM_ERR_INVALID_ARG, "unknown column order");
+    build_incidence(c);
+    build_rows(c, order, c.nodeElemPtr.as<int>(), c.nodeElem.as<int>());
+}
+
+void build_pattern_from_incidence(Context &c, const int *hIndex, const int *hValue) {
+    MFEM_REQUIRE(hIndex && hValue, MFEM_ERR_INVALID_ARG, "null nodeToElem");
+    const int N = c.nbNodes;
+    MFEM_REQUIRE(hIndex[0] == 0, MFEM_ERR_INVALID_ARG, "nodeToElem.index[0] must be 0");
+    for (int i = 0; i < N; i++)
+        MFEM_REQUIRE(hIndex[i + 1] >= hIndex[i], MFEM_ERR_INVALID_ARG,
+                     "nodeToElem.index must be non-decreasing");
+    const long long total = hIndex[N];
+    MFEM_REQUIRE(total <= 64LL * c.nbElem, MFEM_ERR_INVALID_ARG,
+                 "nodeToElem lists more incidences than the mesh can have");
+    DevBuf dptr, dne, raw;
+    int *ptr = (int *)dptr.reserve(sizeof(int) * ((size_t)N + 1));
+    int *ne = (int *)dne.reserve(sizeof(int) * (size_t)std::max(total, 1LL));
+    int *rv = (int *)raw.reserve(sizeof(int) * (size_t)std::max(total, 1LL));
+    MFEM_CUDA(cudaMemcpyAsync(ptr, hIndex, sizeof(int) * ((size_t)N + 1), cudaMemcpyHostToDevice,
+                              c.stream));
+    int *st = status_ptr(c);
+    MFEM_CUDA(cudaMemsetAsync(st, 0, sizeof(int), c.stream));
+    if (total > 0) {
+        MFEM_CUDA(cudaMemcpyAsync(rv, hValue, sizeof(int) * (size_t)total, cudaMemcpyHostToDevice,
+                                  c.stream));
+        k_caller_incidence<<<blocks_for(total, kThreads), kThreads, 0, c.stream>>>(rv, ne, total,
+                                                                                 c.nbElem, st);
+        check_launch("k_caller_incidence");
+    }
+    int bad = 0;
+    read_status(c, &bad, 1);
+    MFEM_REQUIRE(!(bad & kBadIndex), MFEM_ERR_INVALID_ARG,
+                 "nodeToElem holds an element id outside [0, nbElem)");
+    build_rows(c, MFEM_ORDER_REFERENCE, ptr, ne);
+    // the caller's lists are freed on return: the row kernels must be done
+    MFEM_CUDA(cudaStreamSynchronize(c.stream));
 }
 
 __global__ void k_diag_from_pattern(const int *__restrict__ rowPtr, const int *__restrict__ col,

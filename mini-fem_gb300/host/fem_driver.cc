@@ -6,8 +6,11 @@
 //   MINIFEM_DATA_PATH=<root> minifem_fem <mesh> <lap|ela> <iterations>
 //
 // reads <root>/<mesh>/inputs/<op>_1_0 (layout of src/IO.cc:61-96), optionally
-// colours and permutes the elements (MINIFEM_COLORING=1, as the COLORING build
-// does at src/main.cc:209-236), builds the CSR, the Dirichlet mask, runs the
+// colours and permutes the elements in place (MINIFEM_COLORING=1, as the
+// COLORING build does at src/main.cc:209-236), builds the CSR from the
+// node -> element lists (src/main.cc:238-250), optionally the element -> CSR
+// position map (MINIFEM_OPTIMIZED=1, as the OPTIMIZED build does at
+// src/main.cc:319-333), the Dirichlet mask, runs the
 // iterations (iteration 0 untimed when there are several, src/FEM.cc:182) and
 // prints the relative norm differences against <root>/<mesh>/checkings/<op>_1_0
 // (src/FEM.cc:59-98).
@@ -109,6 +112,13 @@ int main(int argc, char **argv) {
     create_nodeToNode(row.data(), col.data(), nodeToElem, e2n.data(), nbNodes);
     if (row[nbNodes] != nbEdges) fail("nbEdges of the mesh file differs from the CSR size");
 
+    std::vector<int> elemToEdge;
+    if (getenv("MINIFEM_OPTIMIZED") && atoi(getenv("MINIFEM_OPTIMIZED"))) {
+        elemToEdge.resize((size_t)nbElem * 16);
+        create_elemToEdge(row.data(), col.data(), e2n.data(), elemToEdge.data(), nbElem);
+        std::cout << "Edges index            : " << elemToEdge.size() << " positions\n";
+    }
+
     // Dirichlet mask: boundary list (src/Fortran/qdmrd4.f) then per-DOF flags
     // (src/Fortran/e_cgmelissa.F: codes 52/53/54 fix x/y/z, other codes fix all)
     std::vector<int> checkBounds((size_t)nbNodes * 3, 0);
@@ -128,8 +138,9 @@ int main(int argc, char **argv) {
     for (int iter = 0; iter < nbIter; iter++) {
         const bool timed = nbIter == 1 || iter > 0;
         if (timed) asmT.start();
-        assembly(coord.data(), values.data(), row.data(), col.data(), e2n.data(), nullptr,
-                 nbElem, nbEdges, operatorDim, operatorID);
+        assembly(coord.data(), values.data(), row.data(), col.data(), e2n.data(),
+                 elemToEdge.empty() ? nullptr : elemToEdge.data(), nbElem, nbEdges, operatorDim,
+                 operatorID);
         if (timed) asmT.stop();
         if (timed) initT.start();
         prec_init(prec.data(), values.data(), row.data(), col.data(), nbNodes, operatorDim);

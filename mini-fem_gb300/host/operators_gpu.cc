@@ -39,8 +39,9 @@ void create_nodeToNode(int *nodeToNodeRow, int *nodeToNodeColumn, index_t &nodeT
     const int nbElem = nodeToElem.index[nbNodes] / 4;
     check(mfem_set_mesh(ctx(), nullptr, elemToNode, nbElem, nbNodes), "create_nodeToNode");
     int nnz = 0;
-    check(mfem_create_nodeToNode(ctx(), MFEM_ORDER_REFERENCE, nodeToNodeRow, nodeToNodeColumn,
-                                 INT_MAX, &nnz),
+    // the columns follow the caller's node -> element order, as src/matrix.cc:66-85 does
+    check(mfem_create_nodeToNode_incidence(ctx(), nodeToElem.index, nodeToElem.value,
+                                           nodeToNodeRow, nodeToNodeColumn, INT_MAX, &nnz),
           "create_nodeToNode");
 }
 

@@ -34,6 +34,7 @@ _SIGS = {
     "mfem_set_mesh": ([_vp, _vp, _vp, C.c_int, C.c_int], C.c_int),
     "mfem_update_coords": ([_vp, _vp], C.c_int),
     "mfem_create_nodeToNode": ([_vp, C.c_int, _vp, _vp, C.c_int, _ip], C.c_int),
+    "mfem_create_nodeToNode_incidence": ([_vp, _vp, _vp, _vp, _vp, C.c_int, _ip], C.c_int),
     "mfem_create_elemToEdge": ([_vp, _vp], C.c_int),
     "mfem_set_pattern": ([_vp, _vp, _vp, C.c_int], C.c_int),
     "mfem_coloring_creation": ([_vp, C.c_ulonglong, _vp, _vp, C.c_int, _ip], C.c_int),

@@ -280,6 +280,17 @@ int orc_threads(void)
 #endif
 }
 
+/* Threads of the parallel loops above: 1 gives the reference's REF build (every
+ * loop serial), the host's core count its OMP/COLORING builds. */
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+    omp_set_num_threads(n > 0 ? n : 1);
+#else
+    (void)n;
+#endif
+}
+
 int orc_prec_inversion(double *prec, const int *row, const int *col,
                        const int *checkBounds, int nbNodes, int operatorID)
 {

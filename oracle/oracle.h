@@ -59,6 +59,7 @@ void orc_prec_init(double *prec, const double *values, const int *row,
  * Returns the number of blocks for which DGETRF/DGETRI reported INFO != 0. */
 /* Threads the OpenMP loops use (1 without OpenMP). */
 int orc_threads(void);
+void orc_set_threads(int n);
 int orc_prec_inversion(double *prec, const int *row, const int *col,
                        const int *checkBounds, int nbNodes, int operatorID);
 

@@ -26,11 +26,29 @@ def build_port() -> str:
     return PORT_SO
 
 
-def build_ref(ref_root: str = "/root/reference") -> bool:
+def ref_root() -> str:
+    """Root of the reference tree: $MINIFEM_REF_ROOT, else the default that the
+    oracle's Makefile names (REF_ROOT), the one place where it is written."""
+    env = os.environ.get("MINIFEM_REF_ROOT")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref-root"], capture_output=True,
+                       text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
+def ref_available() -> bool:
+    """True where the reference sources exist (never on a host without them)."""
+    root = ref_root()
+    return bool(root) and os.path.isdir(os.path.join(root, "src"))
+
+
+def build_ref(root: str | None = None) -> bool:
     """Compile the reference operators where the reference tree exists."""
-    if not os.path.isdir(os.path.join(ref_root, "src")):
+    root = root or ref_root()
+    if not root or not os.path.isdir(os.path.join(root, "src")):
         return False
-    r = subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={ref_root}", "-j4"],
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={root}", "-j4"],
                        capture_output=True, text=True)
     return r.returncode == 0
 
@@ -58,6 +76,8 @@ def port() -> C.CDLL:
         lib.orc_prec_inversion.restype = C.c_int
         lib.orc_threads.argtypes = []
         lib.orc_threads.restype = C.c_int
+        lib.orc_set_threads.argtypes = [C.c_int]
+        lib.orc_set_threads.restype = None
         lib.orc_dqmrd4.argtypes = [C.c_int, _i32p, C.POINTER(C.c_int), _i32p,
                                    C.POINTER(C.c_int)]
         lib.orc_e_essbcm.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _i32p, _i32p]
@@ -74,6 +94,12 @@ def port() -> C.CDLL:
 def threads() -> int:
     """Threads of the port's OpenMP loops (matrix reset, prec_init, prec_inversion)."""
     return int(port().orc_threads())
+
+
+def set_threads(n: int) -> None:
+    """1: the reference's REF build (every loop serial); the host's cores: its
+    OMP/COLORING builds (reset and preconditioner loops in parallel)."""
+    port().orc_set_threads(int(n))
 
 
 def _coef_ptr(coef):
@@ -99,6 +125,30 @@ def pattern(e2n: np.ndarray, nbNodes: int):
     val = np.zeros(4 * E, np.int32)
     lib.orc_node_to_elem(nbNodes, E, e2n, idx, val)
     # an upper bound on the row lengths: 4 * (elements per node)
+    cap = int(np.minimum(np.diff(idx) * 4, nbNodes).sum())
+    row = np.zeros(nbNodes + 1, np.int32)
+    col = np.zeros(max(cap, 1), np.int32)
+    lib.orc_create_nodeToNode(row, col, idx, val, e2n, nbNodes)
+    return row, col[: row[-1]].copy()
+
+
+def node_to_elem(e2n, nbNodes):
+    """(index, value) as DC_create_nodeToElem lists them: ascending element id
+    per node, 0-based element ids (src/main.cc:243-247)."""
+    e2n = np.ascontiguousarray(e2n, dtype=np.int32)
+    idx = np.zeros(nbNodes + 1, np.int32)
+    val = np.zeros(4 * e2n.shape[0], np.int32)
+    port().orc_node_to_elem(nbNodes, e2n.shape[0], e2n, idx, val)
+    return idx, val
+
+
+def pattern_from_incidence(idx, val, e2n, nbNodes):
+    """create_nodeToNode (src/matrix.cc:55-91) over the given node -> element
+    lists, in their order."""
+    lib = port()
+    e2n = np.ascontiguousarray(e2n, dtype=np.int32)
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    val = np.ascontiguousarray(val, dtype=np.int32)
     cap = int(np.minimum(np.diff(idx) * 4, nbNodes).sum())
     row = np.zeros(nbNodes + 1, np.int32)
     col = np.zeros(max(cap, 1), np.int32)

@@ -1,8 +1,9 @@
 """Generate the committed golden fixtures from the reference's own operators.
 
-Run in a checkout that has the reference tree (default /root/reference):
+Run in a checkout that has the reference tree (its root: --ref-root, else
+$MINIFEM_REF_ROOT, else the REF_ROOT default of oracle/Makefile):
 
-    python tests/golden/make_golden.py [--ref-root /root/reference]
+    python tests/golden/make_golden.py [--ref-root <reference root>]
 
 It compiles the reference sources with the stand-ins of oracle/shim (make -C
 oracle ref), runs the reference's create_nodeToNode / create_elemToEdge /
@@ -77,10 +78,10 @@ def make(name: str, mesh: Mesh) -> dict:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", default=None)
     args = ap.parse_args()
     if not O.build_ref(args.ref_root):
-        sys.exit(f"cannot build the reference operators from {args.ref_root}")
+        sys.exit(f"cannot build the reference operators from {args.ref_root or O.ref_root()}")
     O.build_port()
     for name, fn in CASES.items():
         out = make(name, fn())

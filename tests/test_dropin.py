@@ -11,7 +11,7 @@ from conftest import PKG, ROOT
 from minifem.meshgen import cube_mesh, write_reference_tree
 
 DRIVER = os.path.join(PKG, "lib", "minifem_fem")
-REF = os.path.isdir("/root/reference/src")
+REF = O.ref_available()
 
 
 def tree(tmp_path, op, n=6, seed=9):
@@ -72,5 +72,18 @@ def test_driver_with_gpu_colouring(tmp_path):
     tree(tmp_path, "ela")
     out = run(DRIVER, tmp_path, "ela", env={"MINIFEM_COLORING": "1"})
     assert out.returncode == 0, out.stderr
+    d = differences(out.stdout)
+    assert len(d) == 2 and max(d) < 1e-13, out.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("op", ["lap", "ela"])
+def test_driver_optimized_build_flow(tmp_path, op):
+    """src/main.cc with COLORING and OPTIMIZED: colouring, in-place element
+    permutation, CSR from the node -> element lists, create_elemToEdge, FEM loop."""
+    tree(tmp_path, op)
+    out = run(DRIVER, tmp_path, op, env={"MINIFEM_COLORING": "1", "MINIFEM_OPTIMIZED": "1"})
+    assert out.returncode == 0, out.stderr
+    assert "Edges index" in out.stdout
     d = differences(out.stdout)
     assert len(d) == 2 and max(d) < 1e-13, out.stdout

@@ -63,7 +63,7 @@ def test_norm_is_reference_formula():
     assert O.norm(x) == 5.0
 
 
-REF = os.path.isdir("/root/reference/src")
+REF = O.ref_available()
 
 
 @pytest.mark.skipif(not (REF and O.build_ref()), reason="reference tree not present")

@@ -1,6 +1,7 @@
 """mfem_assemble_noalloc: the allocation-free FP64 gather for callers that cannot
-allocate device memory while they assemble (stream-captured CUDA graphs, solvers
-that own all device memory through their own pool, real-time loops).  Its result
+allocate device memory while they assemble (solvers that own all device memory
+through their own pool, loops that cannot afford cudaFree's implicit device
+synchronisation, real-time loops).  Its result
 must equal the allocating entry point's (mfem_assemble, FP64 gather) -- bit for bit,
 the tolerance of the FP64 gather tests -- on two calls in a row.  This file is
 collected last so that a run stopping at the first failure has run everything else."""
