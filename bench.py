@@ -196,6 +196,18 @@ def native_libs_loaded():
                    if ln.split() and ln.split()[-1].endswith(".so") and ROOT in ln.split()[-1]})
 
 
+def max_over_ranks(values, world, device):
+    """Each timing's maximum over the ranks (all_reduce MAX; every rank gets it).
+    `device` is where the reduction tensor lives: the rank's GPU under NCCL,
+    "cpu" under gloo."""
+    if world == 1:
+        return list(values)
+    import torch
+    t = torch.tensor(values, device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import minifem
@@ -379,14 +391,9 @@ def run_ours(args, rank, world, local_rank):
     bt.close()
 
     # maximum over ranks
-    t32 = statistics.mean(ms32)
-    t64 = statistics.mean(ms64)
-    te2e = statistics.mean(e2e_ms)
-    if world > 1:
-        t = torch.tensor([t32, t64, te2e, pipe_ms, pipe64_ms, t_batch],
-                         device=f"cuda:{local_rank}", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t32, t64, te2e, pipe_ms, pipe64_ms, t_batch = t.tolist()
+    t32, t64, te2e, pipe_ms, pipe64_ms, t_batch = max_over_ranks(
+        [statistics.mean(ms32), statistics.mean(ms64), statistics.mean(e2e_ms), pipe_ms, pipe64_ms,
+         t_batch], world, f"cuda:{local_rank}")
     if rank != 0:
         return None
 

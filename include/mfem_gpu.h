@@ -144,6 +144,27 @@ int mfem_prec_inversion(mfem_context *ctx, int *nbSingular);
  * assembly kernels where the strategy allows). */
 int mfem_assemble_prec(mfem_context *ctx, int operatorID, int precision, int strategy);
 
+/* ---- halo: replaces MPI_halo_exchange (src/halo.cc:39-122), the sum of the
+ * interface nodes' preconditioner blocks between sub-domains, called between
+ * prec_init and prec_inversion (src/FEM.cc:211-222). ------------------------ */
+/* The rank's interfaces as src/IO.cc:81-92 reads them: interface i holds the
+ * 1-based local nodes intfNodes[intfIndex[i] .. intfIndex[i+1]), listed in the
+ * same order on both sides.  nbIntf == 0: a single domain (the sum is a
+ * no-op, src/halo.cc:44). */
+int mfem_set_interfaces(mfem_context *ctx, int nbIntf, const int *intfIndex,
+                        const int *intfNodes);
+/* After mfem_prec_init: send[j*opDim + k] = prec block value k of entry j's
+ * node (the reference's bufferSend, src/halo.cc:66-77), a DEVICE buffer of
+ * intfIndex[nbIntf]*opDim doubles, enqueued on the context stream.  The caller
+ * moves slice i (entries intfIndex[i] .. intfIndex[i+1]) to neighbour i and
+ * receives the neighbour's slice into the same place of a receive buffer. */
+int mfem_halo_pack(mfem_context *ctx, double *sendDevice);
+/* prec[node] += recv[entry] for every entry, entries of a node added in
+ * interface order (src/halo.cc:96-112): the reference's bits.  recv is a
+ * DEVICE buffer laid out as the send buffer; enqueued on the context stream.
+ * mfem_prec_inversion follows. */
+int mfem_halo_add(mfem_context *ctx, const double *recvDevice);
+
 /* FP32 precision: elements whose shape quality |6V| / (|a| |b| |c|) (a, b, c the
  * edge vectors from the fourth node) is below `threshold` are integrated in FP64
  * (default 0.1).  *nbFlagged receives the count of the last FP32 assembly. */

@@ -129,6 +129,8 @@ void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int n
     c.gather.built = false;
     c.tiles.built = false;
     c.coloring.built = false;
+    c.halo.built = false;
+    c.precBlocks = false;
     c.coefOp = -1;
     c.hasMask = false;
     c.lastOp = -1;
@@ -204,6 +206,7 @@ void assemble(Context &c, int op, int precision, int strategy, bool fusePrec) {
     MFEM_REQUIRE(precision == MFEM_FP64 || precision == MFEM_FP32, MFEM_ERR_INVALID_ARG, "unknown precision");
     if (strategy == MFEM_AUTO) strategy = MFEM_GATHER;
     MFEM_REQUIRE(strategy >= MFEM_GATHER && strategy <= MFEM_ATOMIC, MFEM_ERR_INVALID_ARG, "unknown strategy");
+    c.precBlocks = false;
     if (precision == MFEM_FP64) assemble_fp64(c, op, strategy, fusePrec);
     else assemble_fp32(c, op, strategy, fusePrec);
     if (fusePrec && !c.precIsInit) {
@@ -520,6 +523,7 @@ int mfem_prec_init(mfem_context *ctx) {
         mfem::pipeline_guard(c);
         mfem::prec_init_fp64(c, c.lastOp);
         c.precIsInit = false;
+        c.precBlocks = true;
     });
 }
 
@@ -531,6 +535,7 @@ int mfem_prec_inversion(mfem_context *ctx, int *nbSingular) {
         int s = mfem::prec_invert(c, c.lastOp);
         if (nbSingular) *nbSingular = s;
         c.precIsInit = true;
+        c.precBlocks = false;
     });
 }
 
@@ -740,6 +745,8 @@ int mfem_prec_init_host(mfem_context *ctx, double *prec, double *nodeToNodeValue
         c.lastOp = op;
         c.lastPrecision = MFEM_FP64;
         mfem::prec_init_fp64(c, op);
+        c.precIsInit = false;
+        c.precBlocks = true;
         MFEM_CUDA(cudaMemcpyAsync(prec, c.prec.as<double>(), sizeof(double) * (size_t)nbNodes * operatorDim,
                                   cudaMemcpyDeviceToHost, c.stream));
         MFEM_CUDA(cudaStreamSynchronize(c.stream));

@@ -44,6 +44,19 @@ struct TilePlan {
     DevBuf w32;                 // per-element weights of the current coefficients
 };
 
+// Interface-node sum of the preconditioner blocks between sub-domains (halo.cu),
+// the device form of src/halo.cc:39-122.  Entry j of the interface lists is
+// node[j]; the distinct interface nodes and, for each, its entries in
+// interface order (the order the reference adds the received blocks in).
+struct HaloPlan {
+    bool built = false;
+    int nbIntf = 0, nbIntfNodes = 0, nUniq = 0;
+    DevBuf node;        // int [nbIntfNodes]  0-based local node of each entry
+    DevBuf uniqNode;    // int [nUniq]
+    DevBuf uniqStart;   // int [nUniq + 1]    into uniqEntry
+    DevBuf uniqEntry;   // int [nbIntfNodes]  entry indices, interface order per node
+};
+
 struct Coloring {
     bool built = false;
     int nbColors = 0;
@@ -137,6 +150,9 @@ struct Context {
     DevBuf values;                    // double or float [nnz * opDim]
     DevBuf prec;                      // double [N * opDim]
     bool precIsInit = false;
+    bool precBlocks = false;          // prec holds the diagonal blocks of the latest
+                                      // assembly, not yet inverted (mfem_prec_init)
+    HaloPlan halo;
 
     // FP32 path: elements whose quality |6V| / (|a||b||c|) is below this
     // threshold get their Jacobian in FP64; the count of the last assembly is
@@ -202,3 +218,26 @@ void read_status(Context &c, int *h, int n);
 struct mfem_context {
     mfem::Context c;
 };
+
+namespace mfem {
+
+// Runs f on the context with its device current and turns internal errors into
+// the status code (message kept for mfem_last_error).
+template <class F>
+int run_guarded(mfem_context *ctx, F &&f) {
+    if (!ctx) return MFEM_ERR_INVALID_ARG;
+    try {
+        MFEM_CUDA(cudaSetDevice(ctx->c.device));
+        f(ctx->c);
+        ctx->c.lastError.clear();
+        return MFEM_OK;
+    } catch (const Error &e) {
+        ctx->c.lastError = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        ctx->c.lastError = "host allocation failed";
+        return MFEM_ERR_CAPACITY;
+    }
+}
+
+}  // namespace mfem

@@ -44,6 +44,9 @@ _SIGS = {
     "mfem_assemble": ([_vp, C.c_int, C.c_int, C.c_int], C.c_int),
     "mfem_assemble_prec": ([_vp, C.c_int, C.c_int, C.c_int], C.c_int),
     "mfem_set_check_bounds": ([_vp, _vp], C.c_int),
+    "mfem_set_interfaces": ([_vp, C.c_int, _vp, _vp], C.c_int),
+    "mfem_halo_pack": ([_vp, _vp], C.c_int),
+    "mfem_halo_add": ([_vp, _vp], C.c_int),
     "mfem_prec_init": ([_vp], C.c_int),
     "mfem_prec_inversion": ([_vp, _ip], C.c_int),
     "mfem_set_sliver_threshold": ([_vp, C.c_double], C.c_int),

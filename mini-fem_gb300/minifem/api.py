@@ -61,6 +61,7 @@ class Assembler:
         if rc != N.MFEM_OK:
             raise N.MfemError(rc, N.lib.mfem_status_string(rc).decode())
         self._h = h
+        self.device = device
         self._keep = {}
         self.nbElem = self.nbNodes = self.nbEdges = 0
         self.op = None

@@ -298,18 +298,125 @@ def bandwidth(elemToNode: np.ndarray) -> int:
     return int((e.max(axis=1) - e.min(axis=1)).max())
 
 
-def write_reference_input(mesh: Mesh, path: str) -> None:
-    """Write `mesh` in the binary layout that src/IO.cc:61-96 reads (one rank,
-    no interfaces)."""
+def _count_nnz(e2n: np.ndarray, nbNodes: int) -> int:
+    e = np.asarray(e2n, dtype=np.int64) - 1
+    a = np.repeat(e, 4, axis=1).reshape(-1)
+    b = np.tile(e, (1, 4)).reshape(-1)
+    return int(np.unique(a * nbNodes + b).size)
+
+
+@dataclass
+class Domain:
+    """One rank's sub-domain in the reference's per-rank input convention
+    (src/IO.cc:61-96, file <op>_<nbBlocks>_<rank>): a mesh with local 1-based
+    ids, and the interfaces with its neighbours -- interface i lists the local
+    nodes shared with rank neighborsList[i] - 1 (src/halo.cc:53-56), in ascending
+    global node order, so both sides list the same nodes in the same order."""
+    mesh: Mesh
+    rank: int
+    nbBlocks: int
+    neighborsList: np.ndarray    # int32 [max(nbIntf, 1) * 3]; first nbIntf: neighbour rank + 1
+    intfIndex: np.ndarray        # int32 [nbIntf + 1]
+    intfNodes: np.ndarray        # int32 [nbIntfNodes], 1-based local nodes
+    globalNode: np.ndarray       # int64 [local nodes]: 0-based global node
+    globalElem: np.ndarray       # int64 [local elements]: global element (ascending)
+
+    @property
+    def nbIntf(self) -> int:
+        return int(self.intfIndex.size - 1)
+
+    @property
+    def neighbors(self) -> np.ndarray:
+        """0-based neighbour rank of each interface."""
+        return self.neighborsList[: self.nbIntf].astype(np.int64) - 1
+
+
+def _bisect(cen: np.ndarray, ids: np.ndarray, parts: int, first: int, part: np.ndarray) -> None:
+    """Recursive coordinate bisection: `parts` blocks numbered from `first`,
+    each cut across the longest extent of the element centroids, the element
+    counts split in proportion to the blocks on each side."""
+    if parts == 1:
+        part[ids] = first
+        return
+    c = cen[ids]
+    axis = int(np.argmax(c.max(axis=0) - c.min(axis=0)))
+    order = ids[np.argsort(c[:, axis], kind="stable")]
+    left = parts // 2
+    cut = (order.size * left) // parts
+    _bisect(cen, order[:cut], left, first, part)
+    _bisect(cen, order[cut:], parts - left, first + left, part)
+
+
+def split_domains(mesh: Mesh, nbBlocks: int) -> list[Domain]:
+    """Element-wise domain decomposition into nbBlocks parts of (nearly) equal
+    element counts by recursive coordinate bisection of the element centroids,
+    as a mesh partitioner would produce the reference's per-rank inputs (four
+    or more parts meet along lines, so some nodes lie on several interfaces).
+    Each rank keeps its elements in ascending global order and its nodes in
+    ascending global order, so a node interior to a rank sums the same
+    contributions in the same order as the undivided mesh."""
+    E, N = mesh.nbElem, mesh.nbNodes
+    e2n0 = np.asarray(mesh.elemToNode, np.int64) - 1
+    cen = mesh.coord[e2n0].mean(axis=1)
+    part = np.empty(E, np.int64)
+    _bisect(cen, np.arange(E), nbBlocks, 0, part)
+    # ranks touching each node (as a bit set, nbBlocks <= 63)
+    if nbBlocks > 63:
+        raise ValueError("at most 63 blocks")
+    touch = np.zeros(N, np.uint64)
+    np.bitwise_or.at(touch, e2n0.reshape(-1), (np.uint64(1) << part.astype(np.uint64)).repeat(4))
+    out = []
+    for p in range(nbBlocks):
+        ge = np.nonzero(part == p)[0]
+        gn = np.unique(e2n0[ge].reshape(-1))
+        local = np.full(N, -1, np.int64)
+        local[gn] = np.arange(gn.size)
+        e2n = (local[e2n0[ge]] + 1).astype(np.int32)
+        neigh, index, nodes = [], [0], []
+        for q in range(nbBlocks):
+            if q == p:
+                continue
+            shared = gn[(touch[gn] >> np.uint64(q)) & np.uint64(1) == 1]
+            if shared.size == 0:
+                continue
+            neigh.append(q + 1)
+            nodes.append(local[shared] + 1)
+            index.append(index[-1] + shared.size)
+        nbIntf = len(neigh)
+        nl = np.zeros(max(nbIntf, 1) * 3, np.int32)
+        nl[:nbIntf] = neigh
+        sub_mesh = Mesh(coord=np.ascontiguousarray(mesh.coord[gn]), elemToNode=e2n,
+                        boundNodesCode=np.ascontiguousarray(mesh.boundNodesCode[gn]),
+                        nbEdges=_count_nnz(e2n, gn.size),
+                        coef=None if mesh.coef is None else np.ascontiguousarray(mesh.coef[ge]),
+                        op=mesh.op, meta=dict(mesh.meta, rank=p, nbBlocks=nbBlocks))
+        out.append(Domain(mesh=sub_mesh, rank=p, nbBlocks=nbBlocks, neighborsList=nl,
+                          intfIndex=np.asarray(index, np.int32),
+                          intfNodes=(np.concatenate(nodes) if nodes else np.zeros(0, np.int64))
+                          .astype(np.int32),
+                          globalNode=gn, globalElem=ge))
+    return out
+
+
+def write_reference_input(mesh: Mesh, path: str, domain: Domain | None = None) -> None:
+    """Write `mesh` in the binary layout that src/IO.cc:61-96 reads; with a
+    domain, its interfaces (neighborsList, intfIndex, intfNodes), else one rank
+    with no interfaces."""
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
-    hdr = np.array([mesh.nbElem, mesh.nbNodes, mesh.nbEdges, 0, 0, mesh.nbBoundNodes],
-                   dtype=np.int32)
+    if domain is None:
+        nl, idx, nodes = np.zeros(3, np.int32), np.zeros(1, np.int32), np.zeros(0, np.int32)
+    else:
+        nl, idx, nodes = domain.neighborsList, domain.intfIndex, domain.intfNodes
+    nbIntf = int(idx.size - 1)
+    hdr = np.array([mesh.nbElem, mesh.nbNodes, mesh.nbEdges, nbIntf, int(nodes.size),
+                    mesh.nbBoundNodes], dtype=np.int32)
     with open(path, "wb") as f:
         f.write(hdr.tobytes())
         f.write(np.ascontiguousarray(mesh.coord, dtype=np.float64).tobytes())
         f.write(np.ascontiguousarray(mesh.elemToNode, dtype=np.int32).tobytes())
-        f.write(np.zeros(3, dtype=np.int32).tobytes())   # neighborsList[max(nbIntf,1)*3]
-        f.write(np.zeros(1, dtype=np.int32).tobytes())   # intfIndex[nbIntf+1]
+        f.write(np.ascontiguousarray(nl, dtype=np.int32).tobytes())      # neighborsList[max(nbIntf,1)*3]
+        f.write(np.ascontiguousarray(idx, dtype=np.int32).tobytes())     # intfIndex[nbIntf+1]
+        f.write(np.ascontiguousarray(nodes, dtype=np.int32).tobytes())   # intfNodes[nbIntfNodes]
         f.write(np.ascontiguousarray(mesh.boundNodesCode, dtype=np.int32).tobytes())
 
 
@@ -326,22 +433,31 @@ def read_reference_input(path: str) -> Mesh:
     coord = np.frombuffer(raw, dtype=np.float64, count=3 * N, offset=off).reshape(N, 3)
     off += 24 * N
     e2n = np.frombuffer(raw, dtype=np.int32, count=4 * E, offset=off).reshape(E, 4)
-    off += 16 * E + max(nbIntf, 1) * 12 + (nbIntf + 1) * 4 + nbIntfNodes * 4
+    off += 16 * E
+    nl = np.frombuffer(raw, dtype=np.int32, count=max(nbIntf, 1) * 3, offset=off)
+    off += max(nbIntf, 1) * 12
+    idx = np.frombuffer(raw, dtype=np.int32, count=nbIntf + 1, offset=off)
+    off += (nbIntf + 1) * 4
+    nodes = np.frombuffer(raw, dtype=np.int32, count=nbIntfNodes, offset=off)
+    off += nbIntfNodes * 4
     code = np.frombuffer(raw, dtype=np.int32, count=N, offset=off)
     return Mesh(coord=coord.copy(), elemToNode=e2n.copy(), boundNodesCode=code.copy(),
-                nbEdges=nnz)
+                nbEdges=nnz, meta={"neighborsList": nl.copy(), "intfIndex": idx.copy(),
+                                   "intfNodes": nodes.copy()})
 
 
 def write_reference_tree(mesh: Mesh, root: str, mesh_name: str, op: str,
                          matrix_norm: float | None = None,
-                         prec_norm: float | None = None) -> str:
-    """Lay out <root>/<mesh_name>/inputs/<op>_1_0 (and checkings/<op>_1_0 when the
-    reference norms are given), the tree the driver reads (src/IO.cc:29-31,
-    :66-68).  Returns the input file path."""
-    path = os.path.join(root, mesh_name, "inputs", f"{op}_1_0")
-    write_reference_input(mesh, path)
+                         prec_norm: float | None = None, domain: Domain | None = None) -> str:
+    """Lay out <root>/<mesh_name>/inputs/<op>_<nbBlocks>_<rank> (and
+    checkings/<op>_<nbBlocks>_<rank> when the reference norms are given), the
+    tree the driver reads (src/IO.cc:29-31, :66-68); one rank (_1_0) without a
+    domain.  Returns the input file path."""
+    tag = f"{op}_1_0" if domain is None else f"{op}_{domain.nbBlocks}_{domain.rank}"
+    path = os.path.join(root, mesh_name, "inputs", tag)
+    write_reference_input(mesh, path, domain)
     if matrix_norm is not None:
-        chk = os.path.join(root, mesh_name, "checkings", f"{op}_1_0")
+        chk = os.path.join(root, mesh_name, "checkings", tag)
         os.makedirs(os.path.dirname(chk), exist_ok=True)
         with open(chk, "w") as f:
             f.write(f"{matrix_norm:.17g}\n{prec_norm:.17g}\n")

@@ -271,6 +271,32 @@ void orc_ela_invert_prec(int nspa, int nnt, const int *innv, const int *nnv,
     for (int k = 0; k < 9; k++) P[k] = a[k];
 }
 
+/* MPI_halo_exchange's two local loops (src/halo.cc:66-77 and :96-112), the
+ * message passing between them left to the caller: the send buffer takes every
+ * interface entry's block before any addition; the received blocks are then
+ * added interface by interface, entry by entry. */
+void orc_halo_pack(const double *prec, const int *intfIndex, const int *intfNodes, int nbIntf,
+                   int operatorDim, double *bufferSend)
+{
+    for (int i = 0; i < nbIntf; i++)
+        for (int j = intfIndex[i]; j < intfIndex[i + 1]; j++) {
+            long tmpNode = intfNodes[j] - 1;
+            for (int k = 0; k < operatorDim; k++)
+                bufferSend[(long)j * operatorDim + k] = prec[tmpNode * operatorDim + k];
+        }
+}
+
+void orc_halo_add(double *prec, const int *intfIndex, const int *intfNodes, int nbIntf,
+                  int operatorDim, const double *bufferRecv)
+{
+    for (int i = 0; i < nbIntf; i++)
+        for (int j = intfIndex[i]; j < intfIndex[i + 1]; j++) {
+            long tmpNode = intfNodes[j] - 1;
+            for (int k = 0; k < operatorDim; k++)
+                prec[tmpNode * operatorDim + k] += bufferRecv[(long)j * operatorDim + k];
+        }
+}
+
 int orc_threads(void)
 {
 #ifdef _OPENMP

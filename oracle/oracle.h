@@ -59,6 +59,10 @@ void orc_prec_init(double *prec, const double *values, const int *row,
  * Returns the number of blocks for which DGETRF/DGETRI reported INFO != 0. */
 /* Threads the OpenMP loops use (1 without OpenMP). */
 int orc_threads(void);
+void orc_halo_pack(const double *prec, const int *intfIndex, const int *intfNodes, int nbIntf,
+                   int operatorDim, double *bufferSend);
+void orc_halo_add(double *prec, const int *intfIndex, const int *intfNodes, int nbIntf,
+                  int operatorDim, const double *bufferRecv);
 void orc_set_threads(int n);
 int orc_prec_inversion(double *prec, const int *row, const int *col,
                        const int *checkBounds, int nbNodes, int operatorID);

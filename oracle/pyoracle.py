@@ -78,6 +78,10 @@ def port() -> C.CDLL:
         lib.orc_threads.restype = C.c_int
         lib.orc_set_threads.argtypes = [C.c_int]
         lib.orc_set_threads.restype = None
+        lib.orc_halo_pack.argtypes = [_f64p, _i32p, _i32p, C.c_int, C.c_int, _f64p]
+        lib.orc_halo_pack.restype = None
+        lib.orc_halo_add.argtypes = [_f64p, _i32p, _i32p, C.c_int, C.c_int, _f64p]
+        lib.orc_halo_add.restype = None
         lib.orc_dqmrd4.argtypes = [C.c_int, _i32p, C.POINTER(C.c_int), _i32p,
                                    C.POINTER(C.c_int)]
         lib.orc_e_essbcm.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _i32p, _i32p]
@@ -208,6 +212,42 @@ def prec(values, row, col, markf, nbNodes, op):
     lib.orc_prec_init(p, values, row, col, nbNodes, d)
     nbad = lib.orc_prec_inversion(p, row, col, markf, nbNodes, op_id(op))
     return p, nbad
+
+
+def prec_blocks(values, row, col, nbNodes, op):
+    """prec_init alone (src/preconditioner.cc:52-87): the diagonal blocks."""
+    d = op_dim(op)
+    p = np.zeros(nbNodes * d, np.float64)
+    port().orc_prec_init(p, values, row, col, nbNodes, d)
+    return p
+
+
+def prec_invert(p, row, col, markf, nbNodes, op):
+    """prec_inversion alone (src/preconditioner.cc:25-49), in place; returns the
+    number of singular blocks."""
+    return port().orc_prec_inversion(p, row, col, np.ascontiguousarray(markf, np.int32), nbNodes,
+                                     op_id(op))
+
+
+def halo_pack(p, intfIndex, intfNodes, op):
+    """The send buffer of MPI_halo_exchange (src/halo.cc:66-77)."""
+    d = op_dim(op)
+    intfIndex = np.ascontiguousarray(intfIndex, np.int32)
+    intfNodes = np.ascontiguousarray(intfNodes, np.int32)
+    nb = len(intfIndex) - 1
+    send = np.zeros(max(int(intfIndex[-1]) * d, 1) if nb > 0 else 1, np.float64)
+    if nb > 0:
+        port().orc_halo_pack(p, intfIndex, intfNodes, nb, d, send)
+    return send[: int(intfIndex[-1]) * d] if nb > 0 else send[:0]
+
+
+def halo_add(p, intfIndex, intfNodes, recv, op):
+    """The additions of MPI_halo_exchange (src/halo.cc:96-112), in place."""
+    intfIndex = np.ascontiguousarray(intfIndex, np.int32)
+    nb = len(intfIndex) - 1
+    if nb > 0:
+        port().orc_halo_add(p, intfIndex, np.ascontiguousarray(intfNodes, np.int32), nb, op_dim(op),
+                            np.ascontiguousarray(recv, np.float64))
 
 
 def getrf_getri3(a_colmajor: np.ndarray):
