@@ -216,13 +216,38 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     mesh = make_mesh(rank)
     E, N = mesh.nbElem, mesh.nbNodes
+    # setup, once per mesh (host wall time, each step synchronised): mesh upload,
+    # CSR pattern, FP32 tile plan, FP64 gather plan (inside the first FP64
+    # assembly, less a steady one), colouring
+    setup = {}
     a = minifem.Assembler(local_rank)
+    t0 = time.perf_counter()
     a.set_mesh(mesh.coord, mesh.elemToNode)
+    a.synchronize()
+    setup["set_mesh_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
     row, col = a.create_nodeToNode("sorted")
+    setup["create_nodeToNode_s"] = time.perf_counter() - t0
     nnz = len(col)
     a.set_coefficients("ela", mesh.coef)
     markf = O.checkbounds(mesh.boundNodesCode)
     a.set_check_bounds(markf)
+    t0 = time.perf_counter()
+    a.tile_info()
+    setup["tile_plan_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a.assembly("ela", "fp64", "gather", prec=True)
+    a.synchronize()
+    first64 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a.assembly("ela", "fp64", "gather", prec=True)
+    a.synchronize()
+    setup["gather_plan_s"] = first64 - (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    ncolors = a.coloring_creation(seed=1)[1].size - 1
+    setup["coloring_s"] = time.perf_counter() - t0
+    setup = {k: round(v, 4) for k, v in setup.items()}
+    setup["colours"] = ncolors
     stream = torch.cuda.ExternalStream(a.stream)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
 
@@ -376,6 +401,13 @@ def run_ours(args, rank, world, local_rank):
         rms.append((s, e))
     torch.cuda.synchronize()
     t_rcm = statistics.mean(x.elapsed_time(y) for x, y in rms)
+    # its accuracy against the FP64 assembly of the same renumbered mesh
+    rrow, rcol = ar.create_nodeToNode("sorted")
+    ar.assembly("ela", "fp32", "gather", prec=True)
+    rv32 = ar.values()
+    ar.assembly("ela", "fp64", "gather", prec=True)
+    rcm_errors = metrics.entry_errors(rrow, rcol, ar.values(), rv32, 9, raw=False)
+    del rv32
     ar.close()
 
     # the batched FP32 form on the same mesh: 8 coefficient sets per iteration,
@@ -388,6 +420,16 @@ def run_ours(args, rank, world, local_rank):
     bt.add(a, "ela", coefs)
     t_batch = _timer(torch, torch.cuda.ExternalStream(bt.stream), flush)(
         lambda: bt.assemble("fp32", prec=True), args.steps, args.warmup)
+    # accuracy of three of the sets against their FP64 assemblies
+    bt.assemble("fp32", prec=True)
+    bt.synchronize()
+    batch_errors = {}
+    for s in (0, n_sets // 2, n_sets - 1):
+        a.set_coefficients("ela", coefs[s])
+        a.assembly("ela", "fp64", "gather", prec=True)
+        batch_errors[f"set_{s}"] = metrics.entry_errors(row, col, a.values(),
+                                                        bt.values(0, s, "fp32"), 9, raw=False)
+    a.set_coefficients("ela", mesh.coef)
     bt.close()
 
     # maximum over ranks
@@ -445,13 +487,16 @@ def run_ours(args, rank, world, local_rank):
         "fp32_over_fp64": round(t64 / t32, 2),
         "fp32_errors_vs_fp64": errors,
         "fp32_rcm": {"value": round(melem(t_rcm), 1), "unit": "Melem/s", "ms_per_step": round(t_rcm, 4),
-                     "renumbering": "reverse Cuthill-McKee (mfem_rcm_permutation)"},
+                     "renumbering": "reverse Cuthill-McKee (mfem_rcm_permutation)",
+                     "errors_vs_fp64": rcm_errors},
         "fp32_batched": {"value": round(n_sets * melem(t_batch), 1), "unit": "Melem/s",
                          "ms_per_step": round(t_batch, 4), "coefficient_sets": n_sets,
                          "counts": "element-assemblies: elements x coefficient sets",
                          "launch": "mfem_batch_assemble: one CUDA graph replay, one persistent tile "
-                                   "kernel over every tile x 8 sets"},
+                                   "kernel over every tile x 8 sets",
+                         "errors_vs_fp64": batch_errors},
         "kernels_ms": prof,
+        "setup": setup,
         "fp64_gradient_evaluations": flagged,
         "e2e": {"value": round(melem(pipe_ms), 1), "unit": "Melem/s", "ms_per_step": round(pipe_ms, 4),
                 "h2d_bytes_per_step": int(hb["coord"].nbytes + hb["coef"].nbytes),
@@ -660,8 +705,10 @@ def run_stress(args):
     flagged = a.flagged()
     slots = a.tile_info()["tile_elems"]
     v32, p32 = a.values(), a.prec()
-    # a stricter quality threshold: more elements take the FP64 gradients
-    a.set_sliver_threshold(0.2)
+    # the threshold the tuner picks for a 1e-6 error target (the lowest that
+    # meets it: fewest FP64 gradient evaluations)
+    from minifem import autotune
+    tuned = autotune.tune_sliver_threshold(a, "ela", row, col, target=1e-6)
     t32q = timed(lambda: a.assembly("ela", "fp32", "gather", prec=True), args.steps, args.warmup)
     flaggedq = a.flagged()
     v32q, p32q = a.values(), a.prec()
@@ -685,10 +732,12 @@ def run_stress(args):
                                "note": "an element is evaluated once per tile that holds it"},
             "fp64_plain": {"value": round(E / (t64 * 1e-3) / 1e6, 1), "ms_per_step": round(t64, 4)},
             "fp32_errors_vs_fp64": err,
-            "quality_threshold_0.2": {"value": round(E / (t32q * 1e-3) / 1e6, 1),
-                                      "ms_per_step": round(t32q, 4),
-                                      "fp64_gradient_fraction": round(flaggedq / slots, 4),
-                                      "fp32_errors_vs_fp64": errq}}
+            "tuned_threshold": {"threshold": tuned["choice"], "target": tuned["target"],
+                                "errors_by_threshold": tuned["errors"],
+                                "value": round(E / (t32q * 1e-3) / 1e6, 1),
+                                "ms_per_step": round(t32q, 4),
+                                "fp64_gradient_fraction": round(flaggedq / slots, 4),
+                                "fp32_errors_vs_fp64": errq}}
 
 
 def run_solve(args):
@@ -774,9 +823,10 @@ def run_batch(args):
     import minifem
     import pyoracle as O
     from minifem.meshgen import cube_mesh, rng_u64
+    from minifem import autotune, metrics
     sides = 12 + (rng_u64(SEED, 99, 64) % np.uint64(49)).astype(int)
     batch = minifem.Batch(0)
-    asms = []
+    asms, patterns, coefs, pending = [], [], [], []
     total_e = total_asm = 0
     for i, n in enumerate(sides):
         op = "lap" if i % 2 == 0 else "ela"
@@ -784,18 +834,42 @@ def run_batch(args):
         m = meshes[0]
         a = minifem.Assembler(0)
         a.set_mesh(m.coord, m.elemToNode)
-        a.create_nodeToNode("sorted")
+        patterns.append(a.create_nodeToNode("sorted"))
         a.set_check_bounds(O.checkbounds(m.boundNodesCode))
-        batch.add(a, op, np.stack([mm.coef for mm in meshes]))
-        asms.append(a)
+        a.set_coefficients(op, m.coef)
+        coefs.append(np.stack([mm.coef for mm in meshes]))
+        # tile size tuned once per (operator, size class of 12 nodes per side)
+        pending.append((a, op, (op, int(n) // 12)))
+        asms.append((a, op))
         total_e += m.nbElem
         total_asm += 8 * m.nbElem
+    t0 = time.perf_counter()
+    choices = autotune.tune_batch_items(pending, repeats=2)
+    tune_s = time.perf_counter() - t0
+    for (a, op), cs in zip(asms, coefs):
+        batch.add(a, op, cs)
     info = batch.info()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
     timed = _timer(torch, torch.cuda.ExternalStream(batch.stream), flush)
     t32 = timed(lambda: batch.assemble("fp32", prec=True), args.steps, args.warmup)
     t64 = timed(lambda: batch.assemble("fp64", prec=True), max(1, args.steps // 2), 1)
     batch.synchronize()
+    # accuracy: FP32 sets of a sample of meshes against the FP64 batch (whose
+    # gather is bit-exact against the oracle), every set of each sampled mesh
+    batch.assemble("fp64", prec=True)
+    batch.synchronize()
+    v64 = {(i, s): batch.values(i, s, "fp64") for i in (0, 1, 62, 63) for s in range(8)}
+    batch.assemble("fp32", prec=True)
+    batch.synchronize()
+    worst = {}
+    for (i, s), ref in v64.items():
+        row, col = patterns[i]
+        e = metrics.entry_errors(row, col, ref, batch.values(i, s, "fp32"), O.op_dim(asms[i][1]),
+                                 raw=False)
+        w = worst.setdefault(f"mesh_{i}_{asms[i][1]}_n{int(sides[i])}", {"max_rel_diag_scaled": 0.0,
+                                                                       "frobenius_rel": 0.0})
+        for k in w:
+            w[k] = max(w[k], e[k])
     return {"metric": "batched assembly + preconditioner, element-assemblies/s (64 meshes x 8 sets)",
             "value": round(total_asm / (t32 * 1e-3) / 1e6, 1), "unit": "Melem/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t32, 4),
@@ -805,9 +879,13 @@ def run_batch(args):
             "config": {"workload": "batch64x8", "meshes": len(sides), "sets": 8,
                        "elements": total_e, "element_assemblies": total_asm,
                        "tiles": info["work"], "persistent_grid": info["grid"],
+                       "tuning": {"tile_size_choices": {f"{op}_n{12 * k}-{12 * k + 11}": c for
+                                                        (_, op, (o, k)), c in zip(pending, choices)},
+                                  "seconds": round(tune_s, 2)},
                        "launch": "one CUDA graph per iteration; FP32 = one persistent kernel"},
             "fp64_plain": {"value": round(total_asm / (t64 * 1e-3) / 1e6, 1),
-                           "ms_per_step": round(t64, 4)}}
+                           "ms_per_step": round(t64, 4)},
+            "fp32_errors_vs_fp64": {"worst_over_8_sets": worst}}
 
 
 def main():

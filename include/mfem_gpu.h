@@ -312,6 +312,11 @@ int mfem_batch_info(mfem_batch *batch, int *nbItems, long long *nbElemTotal,
  * *fastPath = pairs it handled, *mismatches = pairs whose bits differ (0). */
 int mfem_selftest_dmul(mfem_context *ctx, long long n, unsigned long long seed,
                        unsigned long long *fastPath, unsigned long long *mismatches);
+/* Measured FP64 pipe rate of ctx's device (no counterpart in the reference):
+ * kind 0 = additions, 1 = fused multiply-adds, in operations per second (the
+ * best of three timed launches of independent chains on every SM).  The FP64
+ * gather's roofline is this pipe, not HBM. */
+int mfem_fp64_rate(mfem_context *ctx, int kind, double *opsPerSecond);
 
 /* ---- reference-shaped single calls (host buffers in and out) ---------------- */
 /* Same arguments and meaning as the reference operators; each call uploads what

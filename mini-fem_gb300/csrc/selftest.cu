@@ -69,3 +69,58 @@ extern "C" int mfem_selftest_dmul(mfem_context *ctx, long long n, unsigned long 
         return e.code;
     }
 }
+
+// ---- FP64 pipe rate --------------------------------------------------------------
+// The FP64 gather is bound by the FP64 pipe, whose rate the HBM and bf16
+// figures of a roofline do not give.  Every thread advances 8 independent
+// chains of FP64 additions (kind 0) or fused multiply-adds (kind 1) for `iters`
+// steps; operations per second = threads * 8 * iters / elapsed.
+namespace {
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_fp64_rate(int iters, double seed, double *sink) {
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = seed + (double)(threadIdx.x + k);
+    const double b = 1.0000000001, c = 1e-300;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = KIND == 0 ? a[k] + c : fma(a[k], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += a[k];
+    if (s == 12345.678) sink[0] = s;   // keeps the chains; never true in practice
+}
+
+}  // namespace
+
+extern "C" int mfem_fp64_rate(mfem_context *ctx, int kind, double *opsPerSecond) {
+    return mfem::run_guarded(ctx, [&](mfem::Context &c) {
+        MFEM_REQUIRE((kind == 0 || kind == 1) && opsPerSecond, MFEM_ERR_INVALID_ARG,
+                     "kind is 0 (add) or 1 (fma); non-null output");
+        int sms = 0;
+        MFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+        const int blocks = sms * 8, threads = 256, iters = 4096;
+        mfem::DevBuf sink;
+        double *d = (double *)sink.reserve(sizeof(double));
+        cudaEvent_t e0, e1;
+        MFEM_CUDA(cudaEventCreate(&e0));
+        MFEM_CUDA(cudaEventCreate(&e1));
+        float best = 0.f;
+        for (int rep = 0; rep < 4; rep++) {   // the first launch warms up
+            MFEM_CUDA(cudaEventRecord(e0, c.stream));
+            if (kind == 0) k_fp64_rate<0><<<blocks, threads, 0, c.stream>>>(iters, 1.0, d);
+            else k_fp64_rate<1><<<blocks, threads, 0, c.stream>>>(iters, 1.0, d);
+            MFEM_CUDA(cudaEventRecord(e1, c.stream));
+            MFEM_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            MFEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        mfem::check_launch("k_fp64_rate");
+        *opsPerSecond = (double)blocks * threads * 8.0 * iters / (best * 1e-3);
+    });
+}

@@ -70,6 +70,7 @@ _SIGS = {
     "mfem_profile_read": ([_vp, C.c_char_p, C.c_int, _fp, C.c_int, _ip], C.c_int),
     "mfem_get_sizes": ([_vp, _ip, _ip, _ip, _ip], C.c_int),
     "mfem_assemble_noalloc": ([_vp, C.c_int, _vp, _vp, _vp, _vp], C.c_int),
+    "mfem_fp64_rate": ([_vp, C.c_int, C.POINTER(C.c_double)], C.c_int),
     "mfem_selftest_dmul": ([_vp, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong),
                             C.POINTER(C.c_ulonglong)], C.c_int),
     "mfem_batch_create": ([C.POINTER(_vp), C.c_int], C.c_int),

@@ -9,7 +9,12 @@ the only bit-exact one, so a caller that needs bit-exactness keeps it):
 * FP64: strategy gather / atomic / scatter (colour-ordered);
 * node numbering: identity, reverse Cuthill-McKee, Morton or recursive coordinate
   bisection (`tune_renumbering`; the caller applies the permutation, since it
-  renumbers the output).
+  renumbers the output);
+* FP32 sliver threshold (`tune_sliver_threshold`): the lowest quality threshold
+  (fewest FP64 gradient evaluations, so the fastest) whose assembly meets an
+  error target against the mesh's own FP64 assembly;
+* batches (`tune_batch_items`): the FP32 tile size of every distinct mesh shape
+  of a batch, tuned once per shape and applied to each of its contexts.
 
 Each candidate runs `repeats` times after one warm-up; the median of the per-step
 device times (CUDA events recorded by the library around its launches) decides.
@@ -47,9 +52,10 @@ def _time(asm, op, precision, strategy, repeats):
 
 
 def tune(asm, op: str, precision: str, repeats: int = 3, cache: str | None = None,
-         device: int = 0, strategies=None) -> dict:
+         device: int = 0, strategies=None, kernels=(0, 1)) -> dict:
     """Time the candidates on `asm` (mesh, pattern, coefficients already set),
-    apply the fastest and return {"choice": ..., "ms": ..., "timings": [...]}."""
+    apply the fastest and return {"choice": ..., "ms": ..., "timings": [...]}.
+    `kernels` restricts the FP32 kernels tried (the batch runs tiles only)."""
     key = f"{asm.nbElem}:{asm.nbNodes}:{asm.nbEdges}:{op}:{precision}:{_device_name(device)}"
     db = {}
     if cache and os.path.exists(cache):
@@ -60,10 +66,11 @@ def tune(asm, op: str, precision: str, repeats: int = 3, cache: str | None = Non
             return db[key]
     timings = []
     if precision == "fp32":
-        asm.set_option("fp32_kernel", 0)
-        timings.append(({"fp32_kernel": 0, "strategy": "gather"},
-                        _time(asm, op, "fp32", "gather", repeats)))
-        for rows, elems in TILE_CANDIDATES:
+        if 0 in kernels:
+            asm.set_option("fp32_kernel", 0)
+            timings.append(({"fp32_kernel": 0, "strategy": "gather"},
+                            _time(asm, op, "fp32", "gather", repeats)))
+        for rows, elems in (TILE_CANDIDATES if 1 in kernels else ()):
             asm.set_option("fp32_kernel", 1)
             asm.set_option("tile_rows", rows)
             asm.set_option("tile_elems", elems)
@@ -94,6 +101,54 @@ def _apply(asm, choice: dict):
     for k in ("fp32_kernel", "tile_rows", "tile_elems"):
         if k in choice:
             asm.set_option(k, choice[k])
+
+
+THRESHOLDS = (0.05, 0.1, 0.15, 0.2, 0.3, 0.4)
+
+
+def tune_sliver_threshold(asm, op: str, row, col, target: float = 1e-6, repeats: int = 3,
+                          candidates=THRESHOLDS) -> dict:
+    """The lowest FP32 quality threshold whose assembly is within `target` of
+    the FP64 assembly (max entry error relative to the diagonal scale, the
+    measure of minifem.metrics.entry_errors), for the mesh, pattern (row, col as
+    create_nodeToNode returned them) and coefficients already set on `asm`.
+    Applies and returns {"choice", "ms", "errors": {threshold: error}}; if no
+    candidate meets the target, the most accurate one."""
+    from . import metrics
+    dim = 1 if op == "lap" else 9
+    asm.assembly(op, "fp64", "gather", prec=True)
+    ref = asm.values()
+    errors, times = {}, {}
+    for q in sorted(candidates):
+        asm.set_sliver_threshold(q)
+        times[q] = _time(asm, op, "fp32", "gather", repeats)
+        asm.assembly(op, "fp32", "gather", prec=True)
+        errors[q] = metrics.entry_errors(row, col, ref, asm.values(), dim)["max_rel_diag_scaled"]
+        if errors[q] <= target:
+            break
+    ok = [q for q in errors if errors[q] <= target]
+    choice = min(ok) if ok else min(errors, key=errors.get)
+    asm.set_sliver_threshold(choice)
+    return {"choice": choice, "ms": times[choice], "target": target,
+            "errors": {str(q): e for q, e in errors.items()},
+            "timings": {str(q): t for q, t in times.items()}}
+
+
+def tune_batch_items(items, repeats: int = 3, cache: dict | None = None, device: int = 0) -> list:
+    """Tune the FP32 tile size of each (Assembler, op, shape key) in `items`
+    before they are added to a Batch: each distinct shape key (e.g. the cube
+    side and operator) is timed once with `tune` on its first context and the
+    choice applied to every context of that shape.  Returns the choices in item
+    order; `cache` (a dict) carries choices across calls."""
+    cache = {} if cache is None else cache
+    out = []
+    for asm, op, key in items:
+        if key not in cache:
+            cache[key] = tune(asm, op, "fp32", repeats=repeats, device=device,
+                              kernels=(1,))["choice"]
+        _apply(asm, cache[key])
+        out.append(cache[key])
+    return out
 
 
 RENUMBERINGS = ("identity", "rcm", "morton", "bisection")

@@ -6,6 +6,11 @@ matrix with:
 
 * max entry error relative to the diagonal scale, |dA_ij,ab| / sqrt(|A_ii,aa| |A_jj,bb|)
   (a plain relative error is meaningless for entries that cancel to ~0);
+* the raw relative error |dA_ij,ab| / |A_ij,ab| over the values whose magnitude
+  is at least tau times their diagonal scale, for several floors tau, with the
+  count of values above 1e-6 and the share of values the floor keeps (an entry
+  that cancels to 1e-4 of its scale carries the FP32 contributions' relative
+  error times 1e4, whatever the summation);
 * max entry error relative to max |A|;
 * relative Frobenius error ||dA|| / ||A||;
 * relative error of the preconditioned operator P A applied to seeded random
@@ -25,7 +30,7 @@ def _diag_index(row, col):
     return r, pos
 
 
-def entry_errors(row, col, ref, test, dim: int) -> dict:
+def entry_errors(row, col, ref, test, dim: int, raw: bool = True) -> dict:
     R = np.asarray(ref, np.float64).reshape(-1, dim)
     T = np.asarray(test, np.float64).reshape(-1, dim)
     d = np.abs(T - R)
@@ -39,9 +44,32 @@ def entry_errors(row, col, ref, test, dim: int) -> dict:
         scale = np.sqrt(dg[r][:, :, None] * dg[c][:, None, :]).reshape(-1, 9)
     with np.errstate(divide="ignore", invalid="ignore"):
         rel = np.where(scale > 0, d / scale, 0.0)
-    return {"max_rel_diag_scaled": float(rel.max()),
-            "max_rel_to_max": float(d.max() / np.abs(R).max()),
-            "frobenius_rel": float(np.linalg.norm(T - R) / np.linalg.norm(R))}
+    out = {"max_rel_diag_scaled": float(rel.max()),
+           "max_rel_to_max": float(d.max() / np.abs(R).max()),
+           "frobenius_rel": float(np.linalg.norm(T - R) / np.linalg.norm(R))}
+    if raw:
+        out["raw"] = raw_errors(R, d, scale)
+    return out
+
+
+def raw_errors(R, d, scale, floors=(0.1, 0.01, 0.001), bound: float = 1e-6) -> dict:
+    """Raw relative errors |dA| / |A| per value, over the values with |A| >= tau *
+    (diagonal scale) for each floor tau, and over every non-zero value."""
+    A = np.abs(R)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        raw = np.where(A > 0, d / A, 0.0)
+        ratio = np.where(scale > 0, A / scale, np.inf)
+    out = {}
+    for tau in floors:
+        sel = ratio >= tau
+        r = raw[sel]
+        out[f"tau_{tau:g}"] = {"max": float(r.max()) if r.size else 0.0,
+                               "values_above_%g" % bound: int((r > bound).sum()),
+                               "share_of_values": round(float(sel.mean()), 4)}
+    nz = A > 0
+    out["all_nonzero"] = {"max": float(raw[nz].max()), "values_above_%g" % bound: int((raw[nz] > bound).sum()),
+                          "values": int(nz.sum())}
+    return out
 
 
 def _apply(row, col, vals, prec, dim, x):
