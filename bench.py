@@ -147,6 +147,15 @@ def kernel_bytes(name, E, N, nnz, n_edge_units, fp32):
 TRAFFIC_PER_ELEM = {"tile32+prec": (144.148992e6 + 94.183168e6) / 1232274,
                     "edge_units64": (282.084864e6 + 198.790656e6) / 1232274}
 
+# FP64-pipe thread instructions per element of each FP64 gather kernel (ela with
+# coefficients), from one ncu capture of the 60^3 cube
+# (sm__thread_inst_executed_pipe_fp64_pred_on.sum / 1,232,274 tets;
+# profiles/fp64_pipe_ela_cube60.md).  Every count is a fixed number per element,
+# per contribution or per node, so it grows in proportion to the mesh.
+FP64_OPS_PER_ELEM = {"grad64": 73028928 / 1232274,
+                     "diag_units64+prec": 91198720 / 1232274,
+                     "edge_units64": 143159328 / 1232274}
+
 
 _MESHGEN = None
 
@@ -366,6 +375,7 @@ def run_ours(args, rank, world, local_rank):
             agg.setdefault(nme, []).append(t)
         prof[prec] = {k: sum(v) / len(v) for k, v in agg.items()}
     flagged = a.flagged()
+    fp64_peak = a.fp64_rate("add")
 
     # accuracy of the FP32 step against the FP64 one (the FP64 gather equals the
     # oracle bit for bit), untimed
@@ -463,6 +473,23 @@ def run_ours(args, rank, world, local_rank):
 
     r32, s32 = roofline("fp32", t32)
     r64, s64 = roofline("fp64", t64)
+    # the FP64 step against the FP64 pipe, its actual bound: FP64-pipe operations
+    # of the dominant kernel and of the whole step against the measured rate
+    ks64 = prof["fp64"]
+    ops = {k: FP64_OPS_PER_ELEM[k] * E for k in FP64_OPS_PER_ELEM if k in ks64}
+    dom64 = max(ops, key=lambda k: ks64[k])
+    r64["fp64_pipe"] = {
+        "bound": "fp64", "kernel": dom64,
+        "achieved": round(ops[dom64] / (ks64[dom64] * 1e-3) / 1e9, 1),
+        "peak": round(fp64_peak / 1e9, 1), "unit": "Gop/s",
+        "frac": round(ops[dom64] / (ks64[dom64] * 1e-3) / fp64_peak, 4),
+        "ops_per_launch": round(ops[dom64]), "launch_ms": round(ks64[dom64], 4),
+        "step": {"ops": round(sum(ops.values())),
+                 "achieved": round(sum(ops.values()) / (t64 * 1e-3) / 1e9, 1),
+                 "frac": round(sum(ops.values()) / (t64 * 1e-3) / fp64_peak, 4)},
+        "peak_kind": "measured on this GPU by mfem_fp64_rate (independent FP64 additions "
+                     "on every SM, best of 3 launches)",
+        "ops_source": "FP64-pipe thread instructions per element from ncu at 60^3, times E"}
     melem = lambda ms: world * E / (ms * 1e-3) / 1e6  # noqa: E731
     out = {
         "metric": METRIC, "value": round(melem(t32), 1), "unit": "Melem/s", "n_gpus": world,

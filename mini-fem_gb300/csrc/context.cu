@@ -555,7 +555,8 @@ int mfem_set_option(mfem_context *ctx, const char *name, double value) {
             MFEM_REQUIRE(value >= 0.0 && value <= 1.0, MFEM_ERR_INVALID_ARG, "threshold must lie in [0, 1]");
             c.sliverThreshold = (float)value;
         } else if (n == "fp32_kernel") {
-            MFEM_REQUIRE(value == 0.0 || value == 1.0, MFEM_ERR_INVALID_ARG, "fp32_kernel is 0 or 1");
+            MFEM_REQUIRE(value == 0.0 || value == 1.0 || value == 2.0, MFEM_ERR_INVALID_ARG,
+                         "fp32_kernel is 0, 1 or 2");
             c.fp32Kernel = (int)value;
         } else if (n == "tile_rows") {
             MFEM_REQUIRE(value >= 1 && value <= 1024, MFEM_ERR_INVALID_ARG, "tile_rows in [1, 1024]");
@@ -571,6 +572,10 @@ int mfem_set_option(mfem_context *ctx, const char *name, double value) {
         } else if (n == "tile_elems") {
             MFEM_REQUIRE(value >= 64 && value <= 4096, MFEM_ERR_INVALID_ARG, "tile_elems in [64, 4096]");
             c.tiles.maxElem = (int)value;
+            c.tiles.built = false;
+        } else if (n == "unit_order") {
+            MFEM_REQUIRE(value == 0.0 || value == 1.0, MFEM_ERR_INVALID_ARG, "unit_order is 0 or 1");
+            c.tiles.unitOrder = (int)value;
             c.tiles.built = false;
         } else {
             throw Error(MFEM_ERR_INVALID_ARG, "unknown option " + n);

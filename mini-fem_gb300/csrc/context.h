@@ -34,6 +34,10 @@ struct TilePlan {
     bool built = false;
     bool unfit = false;         // built, but the mesh does not fit the tiles
     int maxRows = 48, maxElem = 512;
+    // order of a tile's off-diagonal units: 0 by row, then column; 1 grouped by
+    // the 16-byte alignment of their two block addresses, so that the lanes of
+    // a warp take the same store sequence
+    int unitOrder = 0;
     int nTiles = 0;
     long long nTileElems = 0;   // sum over tiles of their element counts
     long long nUnits = 0;       // off-diagonal units (an intra-tile pair counts once)
@@ -186,6 +190,10 @@ void build_gather_plan(Context &c);
 // tiles.cu
 void build_tile_plan(Context &c);
 void assemble_tiles32(Context &c, int op, bool fusePrec);
+void split_and_weights(Context &c, int op, float4 *hl, float2 *w);
+
+// tile_pipe.cu
+void assemble_tiles32_pipe(Context &c, int op, bool fusePrec);
 TilePlanView plan_view(const TilePlan &tp);
 void split_coords(const Context &c, float4 *hl, cudaStream_t s);
 void weights32_all(int op, const double *coef, long long n, float2 *w, cudaStream_t s);

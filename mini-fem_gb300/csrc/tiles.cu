@@ -200,7 +200,7 @@ void build_tile_plan_impl(Context &c) {
     contrib.reserve((size_t)E * 16 + (size_t)N);
     std::vector<int> mark(E, -1), local(E, 0), elems, rows, cnt, fill, start, keep;
     std::vector<int> rowTile(N, -1), rowLocal(N, 0);
-    std::vector<int> tileNodes, nodeMark(N, -1), nodeLocal(N, 0), tn;
+    std::vector<int> tileNodes, nodeMark(N, -1), nodeLocal(N, 0), tn, posInRow(N, -1);
     std::vector<ushort4> lconn;
     tileNodes.reserve((size_t)N * 4);
     lconn.reserve((size_t)E * 3);
@@ -232,6 +232,14 @@ void build_tile_plan_impl(Context &c) {
         }
         std::sort(elems.begin(), elems.end());
         for (int k = 0; k < (int)elems.size(); k++) local[elems[k]] = k;
+        // element and node segments start on 4-entry boundaries (16-byte aligned
+        // element and node ids, 32-byte aligned connectivity): the pipelined
+        // kernel bulk-copies them
+        while (tileElems.size() % 4) {
+            tileElems.push_back(0);
+            lconn.push_back(make_ushort4(0, 0, 0, 0));
+        }
+        while (tileNodes.size() % 4) tileNodes.push_back(0);
         T.elemBegin = (int)tileElems.size();
         T.nElem = (int)elems.size();
         tileElems.insert(tileElems.end(), elems.begin(), elems.end());
@@ -271,6 +279,8 @@ void build_tile_plan_impl(Context &c) {
                     if (col[row0 + m] == cc) return m;
                 return -1;
             };
+            // position of each column of row r in the row (node-indexed, reset below)
+            for (int m = 0; m < len; m++) posInRow[col[b + m]] = m;
             // which entries of the row this tile computes: the diagonal, entries to
             // rows outside the tile, and (r, c) with c a later row of the tile,
             // which also yields (c, r) transposed
@@ -283,7 +293,7 @@ void build_tile_plan_impl(Context &c) {
             for (int q = nptr[r]; q < nptr[r + 1]; q++) {
                 const int e = nelem[q] >> 2;
                 for (int k = 0; k < 4; k++) {
-                    const int m = where(b, len, e2n[4 * (size_t)e + k]);
+                    const int m = posInRow[e2n[4 * (size_t)e + k]];
                     MFEM_REQUIRE(m >= 0, MFEM_ERR_PATTERN, "tile plan: pattern misses an element pair");
                     cnt[m]++;
                 }
@@ -296,7 +306,7 @@ void build_tile_plan_impl(Context &c) {
             for (int q = nptr[r]; q < nptr[r + 1]; q++) {
                 const int e = nelem[q] >> 2, j = nelem[q] & 3;
                 for (int k = 0; k < 4; k++) {
-                    const int m = where(b, len, e2n[4 * (size_t)e + k]);
+                    const int m = posInRow[e2n[4 * (size_t)e + k]];
                     if (!keep[m]) continue;
                     contrib[T.contribBegin + base + start[m] + fill[m]++] =
                         contrib_code(local[e], j, k);
@@ -323,6 +333,14 @@ void build_tile_plan_impl(Context &c) {
                 }
             }
             if (!hasDiag) diagEnt.push_back(make_int2(r, 0));
+            for (int m = 0; m < len; m++) posInRow[col[b + m]] = -1;
+        }
+        if (tp.unitOrder == 1) {
+            // block p starts at byte 36 p: its 16-byte alignment class is p mod 4;
+            // units of one class give the lanes of a warp the same store sequence
+            auto cls = [](const int4 &u) { return (u.x & 3) * 5 + (u.y < 0 ? 4 : (u.y & 3)); };
+            std::stable_sort(offEnt.begin() + T.offBegin, offEnt.end(),
+                             [&](const int4 &a, const int4 &b) { return cls(a) < cls(b); });
         }
         T.nOff = (int)offEnt.size() - T.offBegin;
         T.nContrib = (int)contrib.size() - T.contribBegin;
@@ -340,6 +358,13 @@ void build_tile_plan_impl(Context &c) {
         maxNodes = std::max(maxNodes, T.nNodes);
         tiles.push_back(T);
     }
+    // the last tile's element and node segments end on 4-entry boundaries too
+    // (the pipelined kernel copies whole 16-byte units)
+    while (tileElems.size() % 4) {
+        tileElems.push_back(0);
+        lconn.push_back(make_ushort4(0, 0, 0, 0));
+    }
+    while (tileNodes.size() % 4) tileNodes.push_back(0);
     MFEM_REQUIRE(tp.maxElem <= 4096, MFEM_ERR_CAPACITY, "tile plan: local index overflow");
 
     tp.nTiles = (int)tiles.size();
@@ -363,10 +388,11 @@ void build_tile_plan_impl(Context &c) {
     up(tp.diagEnt, diagEnt.data(), diagEnt.size() * sizeof(int2));
     up(tp.contrib, contrib.data(), contrib.size() * 2);
     MFEM_CUDA(cudaStreamSynchronize(c.stream));
-    tp.nTileElems = (long long)tileElems.size();
+    tp.nTileElems = 0;
     tp.nUnits = 0;
     tp.nContrib = 0;
     for (const TileDesc &T : tiles) {
+        tp.nTileElems += T.nElem;
         tp.nUnits += T.nOff;
         tp.nContrib += T.nContrib;
     }
@@ -398,6 +424,21 @@ void split_coords(const Context &c, float4 *hl, cudaStream_t s) {
     check_launch("k_split_coords_t");
 }
 
+// The FP32 step's inputs: coordinates split into hi + lo floats and the
+// per-element weights of the current coefficients, one launch.
+void split_and_weights(Context &c, int op, float4 *hl, float2 *w) {
+    const int N = c.nbNodes;
+    c.timer.begin("split_coords+weights", c.stream);
+    const double *coef = c.coefOp == op ? c.coef.as<double>() : nullptr;
+    const unsigned g = blocks_for((long long)N + c.nbElem, 256);
+    if (op == MFEM_OP_LAP)
+        k_split_and_weights<MFEM_OP_LAP><<<g, 256, 0, c.stream>>>(c.coord.as<double>(), N, hl, coef, c.nbElem, w);
+    else
+        k_split_and_weights<MFEM_OP_ELA><<<g, 256, 0, c.stream>>>(c.coord.as<double>(), N, hl, coef, c.nbElem, w);
+    check_launch("k_split_and_weights");
+    c.timer.end(c.stream);
+}
+
 void assemble_tiles32(Context &c, int op, bool fusePrec) {
     build_tile_plan(c);
     const TilePlan &tp = c.tiles;
@@ -407,17 +448,7 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     double *prec = fusePrec ? (double *)c.prec.reserve(sizeof(double) * (size_t)N * dim) : nullptr;
     float4 *hl = (float4 *)c.scratch.reserve(sizeof(float4) * 2 * (size_t)N);
     float2 *w = (float2 *)c.tiles.w32.reserve(sizeof(float2) * (size_t)c.nbElem);
-    c.timer.begin("split_coords+weights", c.stream);
-    {
-        const double *coef = c.coefOp == op ? c.coef.as<double>() : nullptr;
-        const unsigned g = blocks_for((long long)N + c.nbElem, 256);
-        if (op == MFEM_OP_LAP)
-            k_split_and_weights<MFEM_OP_LAP><<<g, 256, 0, c.stream>>>(c.coord.as<double>(), N, hl, coef, c.nbElem, w);
-        else
-            k_split_and_weights<MFEM_OP_ELA><<<g, 256, 0, c.stream>>>(c.coord.as<double>(), N, hl, coef, c.nbElem, w);
-        check_launch("k_split_and_weights");
-    }
-    c.timer.end(c.stream);
+    split_and_weights(c, op, hl, w);
     int *st = status_ptr(c);
     MFEM_CUDA(cudaMemsetAsync(st + 4, 0, sizeof(int) * 3, c.stream));
     TileMesh M;

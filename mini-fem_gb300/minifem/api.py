@@ -186,6 +186,13 @@ class Assembler:
         self._check(N.lib.mfem_selftest_dmul(self._h, n, seed, C.byref(f), C.byref(m)))
         return f.value, m.value
 
+    def fp64_rate(self, kind: str = "add") -> float:
+        """Measured FP64 pipe rate of this context's device, operations per
+        second (kind "add" or "fma")."""
+        r = C.c_double()
+        self._check(N.lib.mfem_fp64_rate(self._h, 0 if kind == "add" else 1, C.byref(r)))
+        return r.value
+
     def flagged(self) -> int:
         n = C.c_int()
         self._check(N.lib.mfem_get_flagged(self._h, C.byref(n)))
