@@ -296,11 +296,10 @@ void launch32(Context &c, bool fusePrec) {
 void assemble_fp32(Context &c, int op, int strategy, bool fusePrec) {
     MFEM_REQUIRE(strategy == MFEM_GATHER, MFEM_ERR_INVALID_ARG,
                  "FP32 assembly offers the gather strategy");
-    if (c.fp32Kernel >= 1) {
+    if (c.fp32Kernel == 1) {
         build_tile_plan(c);
         if (!c.tiles.unfit) {
-            if (c.fp32Kernel == 2) assemble_tiles32_pipe(c, op, fusePrec);
-            else assemble_tiles32(c, op, fusePrec);
+            assemble_tiles32(c, op, fusePrec);
             return;
         }
     }

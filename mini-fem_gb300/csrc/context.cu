@@ -555,8 +555,7 @@ int mfem_set_option(mfem_context *ctx, const char *name, double value) {
             MFEM_REQUIRE(value >= 0.0 && value <= 1.0, MFEM_ERR_INVALID_ARG, "threshold must lie in [0, 1]");
             c.sliverThreshold = (float)value;
         } else if (n == "fp32_kernel") {
-            MFEM_REQUIRE(value == 0.0 || value == 1.0 || value == 2.0, MFEM_ERR_INVALID_ARG,
-                         "fp32_kernel is 0, 1 or 2");
+            MFEM_REQUIRE(value == 0.0 || value == 1.0, MFEM_ERR_INVALID_ARG, "fp32_kernel is 0 or 1");
             c.fp32Kernel = (int)value;
         } else if (n == "tile_rows") {
             MFEM_REQUIRE(value >= 1 && value <= 1024, MFEM_ERR_INVALID_ARG, "tile_rows in [1, 1024]");

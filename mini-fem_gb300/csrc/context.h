@@ -191,9 +191,6 @@ void build_gather_plan(Context &c);
 void build_tile_plan(Context &c);
 void assemble_tiles32(Context &c, int op, bool fusePrec);
 void split_and_weights(Context &c, int op, float4 *hl, float2 *w);
-
-// tile_pipe.cu
-void assemble_tiles32_pipe(Context &c, int op, bool fusePrec);
 TilePlanView plan_view(const TilePlan &tp);
 void split_coords(const Context &c, float4 *hl, cudaStream_t s);
 void weights32_all(int op, const double *coef, long long n, float2 *w, cudaStream_t s);

@@ -232,14 +232,6 @@ void build_tile_plan_impl(Context &c) {
         }
         std::sort(elems.begin(), elems.end());
         for (int k = 0; k < (int)elems.size(); k++) local[elems[k]] = k;
-        // element and node segments start on 4-entry boundaries (16-byte aligned
-        // element and node ids, 32-byte aligned connectivity): the pipelined
-        // kernel bulk-copies them
-        while (tileElems.size() % 4) {
-            tileElems.push_back(0);
-            lconn.push_back(make_ushort4(0, 0, 0, 0));
-        }
-        while (tileNodes.size() % 4) tileNodes.push_back(0);
         T.elemBegin = (int)tileElems.size();
         T.nElem = (int)elems.size();
         tileElems.insert(tileElems.end(), elems.begin(), elems.end());
@@ -358,13 +350,6 @@ void build_tile_plan_impl(Context &c) {
         maxNodes = std::max(maxNodes, T.nNodes);
         tiles.push_back(T);
     }
-    // the last tile's element and node segments end on 4-entry boundaries too
-    // (the pipelined kernel copies whole 16-byte units)
-    while (tileElems.size() % 4) {
-        tileElems.push_back(0);
-        lconn.push_back(make_ushort4(0, 0, 0, 0));
-    }
-    while (tileNodes.size() % 4) tileNodes.push_back(0);
     MFEM_REQUIRE(tp.maxElem <= 4096, MFEM_ERR_CAPACITY, "tile plan: local index overflow");
 
     tp.nTiles = (int)tiles.size();

@@ -76,20 +76,4 @@ struct SmemLayout {
 };
 
 SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes);
-
-// Shared memory of the pipelined tile kernel (tile_pipe.cu): the gradients,
-// row results and flagged-element queue once, and two input buffers -- the
-// tile being computed and the next one, being copied in -- each holding the
-// plan segments (contribution lists, diagonal and off-diagonal tables, element
-// ids, connectivity, node ids), the gathered node coordinates (hi parts, then
-// lo parts) and the gathered weights.  Offsets in bytes; buffer k starts at
-// buf + k * bufBytes.
-struct PipeLayout {
-    int g, res, q, bar, buf, bufBytes, bytes;
-    int contrib, diag, off, elems, lconn, nodes, x, w;   // within a buffer
-    int maxNodes;                                          // lo parts at x + 16 * maxNodes
-};
-
-PipeLayout pipe_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRowsPad, int maxNodes);
-
 }  // namespace mfem
