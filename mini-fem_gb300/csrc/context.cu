@@ -572,10 +572,6 @@ int mfem_set_option(mfem_context *ctx, const char *name, double value) {
             MFEM_REQUIRE(value >= 64 && value <= 4096, MFEM_ERR_INVALID_ARG, "tile_elems in [64, 4096]");
             c.tiles.maxElem = (int)value;
             c.tiles.built = false;
-        } else if (n == "unit_order") {
-            MFEM_REQUIRE(value == 0.0 || value == 1.0, MFEM_ERR_INVALID_ARG, "unit_order is 0 or 1");
-            c.tiles.unitOrder = (int)value;
-            c.tiles.built = false;
         } else {
             throw Error(MFEM_ERR_INVALID_ARG, "unknown option " + n);
         }

@@ -34,10 +34,6 @@ struct TilePlan {
     bool built = false;
     bool unfit = false;         // built, but the mesh does not fit the tiles
     int maxRows = 48, maxElem = 512;
-    // order of a tile's off-diagonal units: 0 by row, then column; 1 grouped by
-    // the 16-byte alignment of their two block addresses, so that the lanes of
-    // a warp take the same store sequence
-    int unitOrder = 0;
     int nTiles = 0;
     long long nTileElems = 0;   // sum over tiles of their element counts
     long long nUnits = 0;       // off-diagonal units (an intra-tile pair counts once)

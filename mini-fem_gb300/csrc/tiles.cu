@@ -327,13 +327,6 @@ void build_tile_plan_impl(Context &c) {
             if (!hasDiag) diagEnt.push_back(make_int2(r, 0));
             for (int m = 0; m < len; m++) posInRow[col[b + m]] = -1;
         }
-        if (tp.unitOrder == 1) {
-            // block p starts at byte 36 p: its 16-byte alignment class is p mod 4;
-            // units of one class give the lanes of a warp the same store sequence
-            auto cls = [](const int4 &u) { return (u.x & 3) * 5 + (u.y < 0 ? 4 : (u.y & 3)); };
-            std::stable_sort(offEnt.begin() + T.offBegin, offEnt.end(),
-                             [&](const int4 &a, const int4 &b) { return cls(a) < cls(b); });
-        }
         T.nOff = (int)offEnt.size() - T.offBegin;
         T.nContrib = (int)contrib.size() - T.contribBegin;
         // pad every segment so that the next tile starts 16-byte aligned and
