@@ -29,8 +29,11 @@
 // contribution list is in ascending element order and every combination order
 // is fixed, so results are deterministic.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
+#include <exception>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "context.h"
@@ -154,20 +157,31 @@ void build_tile_plan(Context &c) {
 
 namespace {
 
+// The plan is built in three passes: the rows in Morton order are cut into
+// tiles (sequential: a tile grows while its rows' elements fit), every tile's
+// lists are then built independently on all host threads, and the per-tile
+// lists are finally laid end to end with the padding the bulk copies need.
+struct TileLists {
+    std::vector<int> elems, nodes;
+    std::vector<ushort4> lconn;
+    std::vector<unsigned short> contrib;
+    std::vector<int2> diag;
+    std::vector<int4> off;
+};
+
 void build_tile_plan_impl(Context &c) {
     TilePlan &tp = c.tiles;
     build_incidence(c);
     const int N = c.nbNodes, E = c.nbElem, nnz = c.nnz;
     std::vector<double> coord((size_t)N * 3);
     std::vector<int> e2n((size_t)E * 4), nptr(N + 1), nelem((size_t)E * 4), rowPtr(N + 1),
-        col((size_t)nnz), diagPos(N);
+        col((size_t)nnz);
     MFEM_CUDA(cudaMemcpyAsync(coord.data(), c.coord.ptr, coord.size() * 8, cudaMemcpyDeviceToHost, c.stream));
     MFEM_CUDA(cudaMemcpyAsync(e2n.data(), c.e2n.ptr, e2n.size() * 4, cudaMemcpyDeviceToHost, c.stream));
     MFEM_CUDA(cudaMemcpyAsync(nptr.data(), c.nodeElemPtr.ptr, nptr.size() * 4, cudaMemcpyDeviceToHost, c.stream));
     MFEM_CUDA(cudaMemcpyAsync(nelem.data(), c.nodeElem.ptr, nelem.size() * 4, cudaMemcpyDeviceToHost, c.stream));
     MFEM_CUDA(cudaMemcpyAsync(rowPtr.data(), c.rowPtr.ptr, rowPtr.size() * 4, cudaMemcpyDeviceToHost, c.stream));
     MFEM_CUDA(cudaMemcpyAsync(col.data(), c.col.ptr, col.size() * 4, cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaMemcpyAsync(diagPos.data(), c.diagPos.ptr, diagPos.size() * 4, cudaMemcpyDeviceToHost, c.stream));
     MFEM_CUDA(cudaStreamSynchronize(c.stream));
 
     // Morton order of the nodes (10 bits per axis over the bounding box)
@@ -190,87 +204,68 @@ void build_tile_plan_impl(Context &c) {
     }
     std::sort(key.begin(), key.end());
 
-    std::vector<TileDesc> tiles;
-    std::vector<int> tileElems;
-    std::vector<int4> offEnt;
-    std::vector<int2> diagEnt;
-    std::vector<unsigned short> contrib;
-    offEnt.reserve((size_t)nnz + N);
-    diagEnt.reserve((size_t)N * 2);
-    contrib.reserve((size_t)E * 16 + (size_t)N);
-    std::vector<int> mark(E, -1), local(E, 0), elems, rows, cnt, fill, start, keep;
-    std::vector<int> rowTile(N, -1), rowLocal(N, 0);
-    std::vector<int> tileNodes, nodeMark(N, -1), nodeLocal(N, 0), tn, posInRow(N, -1);
-    std::vector<ushort4> lconn;
-    tileNodes.reserve((size_t)N * 4);
-    lconn.reserve((size_t)E * 3);
-    int maxElem = 0, maxContrib = 0, maxOff = 0, maxRows = 0, maxNodes = 0;
+    // 1. the cut: consecutive rows while the tile's incident elements fit
+    std::vector<int> tileRowBegin, rowOrder(N), rowTile(N, -1), rowLocal(N, 0), mark(E, -1);
+    {
+        int i = 0, elemCount = 0;
+        while (i < N) {
+            const int t = (int)tileRowBegin.size();
+            tileRowBegin.push_back(i);
+            elemCount = 0;
+            int nr = 0;
+            while (i < N && nr < tp.maxRows) {
+                const int r = (int)(key[i] & 0xffffffffu);
+                int add = 0;
+                for (int q = nptr[r]; q < nptr[r + 1]; q++)
+                    if (mark[nelem[q] >> 2] != t) add++;
+                if (nr > 0 && elemCount + add > tp.maxElem) break;
+                MFEM_REQUIRE(elemCount + add <= tp.maxElem, MFEM_ERR_CAPACITY,
+                             "tile plan: one row touches more elements than a tile holds");
+                for (int q = nptr[r]; q < nptr[r + 1]; q++) mark[nelem[q] >> 2] = t;
+                elemCount += add;
+                rowOrder[i] = r;
+                rowTile[r] = t;
+                rowLocal[r] = nr++;
+                i++;
+            }
+        }
+        tileRowBegin.push_back(N);
+    }
+    MFEM_REQUIRE(tp.maxElem <= 4096, MFEM_ERR_CAPACITY, "tile plan: local index overflow");
+    const int nTiles = (int)tileRowBegin.size() - 1;
 
-    int i = 0;
-    while (i < N) {
-        const int tIndex = (int)tiles.size();
-        TileDesc T{};
-        elems.clear();
-        rows.clear();
-        while (i < N && (int)rows.size() < tp.maxRows) {
-            const int r = (int)(key[i] & 0xffffffffu);
-            int add = 0;
-            for (int q = nptr[r]; q < nptr[r + 1]; q++)
-                if (mark[nelem[q] >> 2] != tIndex) add++;
-            if (!rows.empty() && (int)elems.size() + add > tp.maxElem) break;
-            MFEM_REQUIRE((int)elems.size() + add <= tp.maxElem, MFEM_ERR_CAPACITY,
-                         "tile plan: one row touches more elements than a tile holds");
-            for (int q = nptr[r]; q < nptr[r + 1]; q++) {
-                const int e = nelem[q] >> 2;
-                if (mark[e] != tIndex) {
-                    mark[e] = tIndex;
-                    elems.push_back(e);
-                }
-            }
-            rows.push_back(r);
-            i++;
+    // 2. every tile's lists, tiles spread over the host threads
+    std::vector<TileLists> lists(nTiles);
+    auto buildTile = [&](int t, std::vector<int> &posInRow) {
+        TileLists &L = lists[t];
+        const int r0 = tileRowBegin[t], nRows = tileRowBegin[t + 1] - r0;
+        for (int lr = 0; lr < nRows; lr++) {
+            const int r = rowOrder[r0 + lr];
+            for (int q = nptr[r]; q < nptr[r + 1]; q++) L.elems.push_back(nelem[q] >> 2);
         }
-        std::sort(elems.begin(), elems.end());
-        for (int k = 0; k < (int)elems.size(); k++) local[elems[k]] = k;
-        T.elemBegin = (int)tileElems.size();
-        T.nElem = (int)elems.size();
-        tileElems.insert(tileElems.end(), elems.begin(), elems.end());
-        // the nodes of the tile's elements, and the elements' nodes as indices into them
-        tn.clear();
-        for (int e : elems)
-            for (int k = 0; k < 4; k++) {
-                const int n = e2n[4 * (size_t)e + k];
-                if (nodeMark[n] != tIndex) {
-                    nodeMark[n] = tIndex;
-                    tn.push_back(n);
-                }
-            }
-        std::sort(tn.begin(), tn.end());
-        for (int k = 0; k < (int)tn.size(); k++) nodeLocal[tn[k]] = k;
-        T.nodeBegin = (int)tileNodes.size();
-        T.nNodes = (int)tn.size();
-        tileNodes.insert(tileNodes.end(), tn.begin(), tn.end());
-        for (int e : elems) {
+        std::sort(L.elems.begin(), L.elems.end());
+        L.elems.erase(std::unique(L.elems.begin(), L.elems.end()), L.elems.end());
+        for (int e : L.elems)
+            for (int k = 0; k < 4; k++) L.nodes.push_back(e2n[4 * (size_t)e + k]);
+        std::sort(L.nodes.begin(), L.nodes.end());
+        L.nodes.erase(std::unique(L.nodes.begin(), L.nodes.end()), L.nodes.end());
+        auto nodeLocal = [&](int n) {
+            return (unsigned short)(std::lower_bound(L.nodes.begin(), L.nodes.end(), n) - L.nodes.begin());
+        };
+        auto elemLocal = [&](int e) {
+            return (int)(std::lower_bound(L.elems.begin(), L.elems.end(), e) - L.elems.begin());
+        };
+        L.lconn.reserve(L.elems.size());
+        for (int e : L.elems) {
             const size_t b4 = 4 * (size_t)e;
-            lconn.push_back(make_ushort4((unsigned short)nodeLocal[e2n[b4]], (unsigned short)nodeLocal[e2n[b4 + 1]],
-                                         (unsigned short)nodeLocal[e2n[b4 + 2]], (unsigned short)nodeLocal[e2n[b4 + 3]]));
+            L.lconn.push_back(make_ushort4(nodeLocal(e2n[b4]), nodeLocal(e2n[b4 + 1]),
+                                           nodeLocal(e2n[b4 + 2]), nodeLocal(e2n[b4 + 3])));
         }
-        T.offBegin = (int)offEnt.size();
-        T.diagBegin = (int)diagEnt.size();
-        T.contribBegin = (int)contrib.size();
-        T.nRows = (int)rows.size();
-        for (int k = 0; k < T.nRows; k++) {
-            rowTile[rows[k]] = tIndex;
-            rowLocal[rows[k]] = k;
-        }
-        for (int lr = 0; lr < T.nRows; lr++) {
-            const int r = rows[lr];
+        std::vector<int> cnt, start, fill;
+        std::vector<char> keep;
+        for (int lr = 0; lr < nRows; lr++) {
+            const int r = rowOrder[r0 + lr];
             const int b = rowPtr[r], len = rowPtr[r + 1] - b;
-            auto where = [&](int row0, int rowLen, int cc) {
-                for (int m = 0; m < rowLen; m++)
-                    if (col[row0 + m] == cc) return m;
-                return -1;
-            };
             // position of each column of row r in the row (node-indexed, reset below)
             for (int m = 0; m < len; m++) posInRow[col[b + m]] = m;
             // which entries of the row this tile computes: the diagonal, entries to
@@ -279,7 +274,7 @@ void build_tile_plan_impl(Context &c) {
             keep.assign(len, 0);
             for (int m = 0; m < len; m++) {
                 const int cc = col[b + m];
-                keep[m] = cc == r || rowTile[cc] != tIndex || rowLocal[cc] > lr;
+                keep[m] = cc == r || rowTile[cc] != t || rowLocal[cc] > lr;
             }
             cnt.assign(len, 0);
             for (int q = nptr[r]; q < nptr[r + 1]; q++) {
@@ -292,16 +287,15 @@ void build_tile_plan_impl(Context &c) {
             }
             start.assign(len + 1, 0);
             for (int m = 0; m < len; m++) start[m + 1] = start[m] + (keep[m] ? cnt[m] : 0);
-            const int base = (int)contrib.size() - T.contribBegin;
-            contrib.resize(contrib.size() + start[len]);
+            const int base = (int)L.contrib.size();
+            L.contrib.resize(L.contrib.size() + start[len]);
             fill.assign(len, 0);
             for (int q = nptr[r]; q < nptr[r + 1]; q++) {
                 const int e = nelem[q] >> 2, j = nelem[q] & 3;
                 for (int k = 0; k < 4; k++) {
                     const int m = posInRow[e2n[4 * (size_t)e + k]];
                     if (!keep[m]) continue;
-                    contrib[T.contribBegin + base + start[m] + fill[m]++] =
-                        contrib_code(local[e], j, k);
+                    L.contrib[base + start[m] + fill[m]++] = contrib_code(elemLocal(e), j, k);
                 }
             }
             bool hasDiag = false;
@@ -312,25 +306,87 @@ void build_tile_plan_impl(Context &c) {
                 const int meta = ((base + start[m]) << 8) | cnt[m];
                 const int cc = col[b + m];
                 if (cc == r) {
-                    diagEnt.push_back(make_int2(r, meta));
+                    L.diag.push_back(make_int2(r, meta));
                     hasDiag = true;
                 } else {
                     int tpos = -1;
-                    if (rowTile[cc] == tIndex) {
-                        const int tm = where(rowPtr[cc], rowPtr[cc + 1] - rowPtr[cc], r);
-                        MFEM_REQUIRE(tm >= 0, MFEM_ERR_PATTERN, "tile plan: pattern is not symmetric");
-                        tpos = rowPtr[cc] + tm;
+                    if (rowTile[cc] == t) {
+                        const int cb = rowPtr[cc], clen = rowPtr[cc + 1] - cb;
+                        for (int mm = 0; mm < clen; mm++)
+                            if (col[cb + mm] == r) { tpos = cb + mm; break; }
+                        MFEM_REQUIRE(tpos >= 0, MFEM_ERR_PATTERN, "tile plan: pattern is not symmetric");
                     }
-                    offEnt.push_back(make_int4(b + m, tpos, meta, 0));
+                    L.off.push_back(make_int4(b + m, tpos, meta, 0));
                 }
             }
-            if (!hasDiag) diagEnt.push_back(make_int2(r, 0));
+            if (!hasDiag) L.diag.push_back(make_int2(r, 0));
             for (int m = 0; m < len; m++) posInRow[col[b + m]] = -1;
         }
-        T.nOff = (int)offEnt.size() - T.offBegin;
-        T.nContrib = (int)contrib.size() - T.contribBegin;
-        // pad every segment so that the next tile starts 16-byte aligned and
-        // the bulk copies move whole 16-byte units that lie inside the arrays
+    };
+    {
+        const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+        const int nThreads = (int)std::min<long long>(hw, std::max(1, nTiles / 16));
+        std::atomic<int> nextTile(0);
+        std::vector<std::exception_ptr> errs(nThreads);
+        auto worker = [&](int w) {
+            try {
+                std::vector<int> posInRow(N, -1);
+                for (int t; (t = nextTile.fetch_add(1)) < nTiles;) buildTile(t, posInRow);
+            } catch (...) {
+                errs[w] = std::current_exception();
+                nextTile.store(nTiles);
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int w = 1; w < nThreads; w++) pool.emplace_back(worker, w);
+        worker(0);
+        for (auto &th : pool) th.join();
+        for (auto &e : errs)
+            if (e) std::rethrow_exception(e);
+    }
+
+    // 3. the lists end to end; every segment starts 16-byte aligned and is padded
+    // to whole 16-byte units that lie inside the arrays (one bulk copy each)
+    std::vector<TileDesc> tiles(nTiles);
+    size_t nE = 0, nN = 0, nC = 0, nD = 0, nO = 0;
+    for (const TileLists &L : lists) {
+        nE += L.elems.size();
+        nN += L.nodes.size();
+        nC += L.contrib.size() + 8;
+        nD += L.diag.size() + 1;
+        nO += L.off.size();
+    }
+    std::vector<int> tileElems, tileNodes;
+    std::vector<ushort4> lconn;
+    std::vector<unsigned short> contrib;
+    std::vector<int2> diagEnt;
+    std::vector<int4> offEnt;
+    tileElems.reserve(nE);
+    lconn.reserve(nE);
+    tileNodes.reserve(nN);
+    contrib.reserve(nC);
+    diagEnt.reserve(nD);
+    offEnt.reserve(nO);
+    int maxElem = 0, maxContrib = 0, maxOff = 0, maxRows = 0, maxNodes = 0;
+    for (int t = 0; t < nTiles; t++) {
+        TileLists &L = lists[t];
+        TileDesc &T = tiles[t];
+        T.elemBegin = (int)tileElems.size();
+        T.nElem = (int)L.elems.size();
+        tileElems.insert(tileElems.end(), L.elems.begin(), L.elems.end());
+        lconn.insert(lconn.end(), L.lconn.begin(), L.lconn.end());
+        T.nodeBegin = (int)tileNodes.size();
+        T.nNodes = (int)L.nodes.size();
+        tileNodes.insert(tileNodes.end(), L.nodes.begin(), L.nodes.end());
+        T.offBegin = (int)offEnt.size();
+        T.diagBegin = (int)diagEnt.size();
+        T.contribBegin = (int)contrib.size();
+        T.nRows = tileRowBegin[t + 1] - tileRowBegin[t];
+        offEnt.insert(offEnt.end(), L.off.begin(), L.off.end());
+        diagEnt.insert(diagEnt.end(), L.diag.begin(), L.diag.end());
+        contrib.insert(contrib.end(), L.contrib.begin(), L.contrib.end());
+        T.nOff = (int)L.off.size();
+        T.nContrib = (int)L.contrib.size();
         while (diagEnt.size() % 2) diagEnt.push_back(make_int2(0, 0));
         while (contrib.size() % 8) contrib.push_back(0);
         T.nOffPad = (int)offEnt.size() - T.offBegin;
@@ -341,9 +397,8 @@ void build_tile_plan_impl(Context &c) {
         maxOff = std::max(maxOff, T.nOffPad);
         maxRows = std::max(maxRows, T.nRowsPad);
         maxNodes = std::max(maxNodes, T.nNodes);
-        tiles.push_back(T);
+        L = TileLists();   // release as we go
     }
-    MFEM_REQUIRE(tp.maxElem <= 4096, MFEM_ERR_CAPACITY, "tile plan: local index overflow");
 
     tp.nTiles = (int)tiles.size();
     tp.layout = smem_layout(std::max(maxElem, 1), maxContrib, maxOff, maxRows, maxNodes);
