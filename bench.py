@@ -865,13 +865,13 @@ def run_batch(args):
         a.set_check_bounds(O.checkbounds(m.boundNodesCode))
         a.set_coefficients(op, m.coef)
         coefs.append(np.stack([mm.coef for mm in meshes]))
-        # tile size tuned once per (operator, size class of 12 nodes per side)
-        pending.append((a, op, (op, int(n) // 12)))
+        pending.append((a, op, coefs[-1]))
         asms.append((a, op))
         total_e += m.nbElem
         total_asm += 8 * m.nbElem
+    # one tile size for the whole batch, timed on the batch
     t0 = time.perf_counter()
-    choices = autotune.tune_batch_items(pending, repeats=2)
+    tuned = autotune.tune_batch(pending, repeats=3)
     tune_s = time.perf_counter() - t0
     for (a, op), cs in zip(asms, coefs):
         batch.add(a, op, cs)
@@ -906,8 +906,9 @@ def run_batch(args):
             "config": {"workload": "batch64x8", "meshes": len(sides), "sets": 8,
                        "elements": total_e, "element_assemblies": total_asm,
                        "tiles": info["work"], "persistent_grid": info["grid"],
-                       "tuning": {"tile_size_choices": {f"{op}_n{12 * k}-{12 * k + 11}": c for
-                                                        (_, op, (o, k)), c in zip(pending, choices)},
+                       "tuning": {"tile_size": tuned["choice"],
+                                  "candidates_ms": [[f"{c['tile_rows']}x{c['tile_elems']}", round(t, 3)]
+                                                    for c, t in tuned["timings"]],
                                   "seconds": round(tune_s, 2)},
                        "launch": "one CUDA graph per iteration; FP32 = one persistent kernel"},
             "fp64_plain": {"value": round(total_asm / (t64 * 1e-3) / 1e6, 1),

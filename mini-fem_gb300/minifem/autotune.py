@@ -13,8 +13,9 @@ the only bit-exact one, so a caller that needs bit-exactness keeps it):
 * FP32 sliver threshold (`tune_sliver_threshold`): the lowest quality threshold
   (fewest FP64 gradient evaluations, so the fastest) whose assembly meets an
   error target against the mesh's own FP64 assembly;
-* batches (`tune_batch_items`): the FP32 tile size of every distinct mesh shape
-  of a batch, tuned once per shape and applied to each of its contexts.
+* batches (`tune_batch`): one FP32 tile size for all meshes of a batch, timed on
+  the whole batch (its persistent kernel sizes shared memory for the largest
+  tile of any mesh).
 
 Each candidate runs `repeats` times after one warm-up; the median of the per-step
 device times (CUDA events recorded by the library around its launches) decides.
@@ -134,21 +135,50 @@ def tune_sliver_threshold(asm, op: str, row, col, target: float = 1e-6, repeats:
             "timings": {str(q): t for q, t in times.items()}}
 
 
-def tune_batch_items(items, repeats: int = 3, cache: dict | None = None, device: int = 0) -> list:
-    """Tune the FP32 tile size of each (Assembler, op, shape key) in `items`
-    before they are added to a Batch: each distinct shape key (e.g. the cube
-    side and operator) is timed once with `tune` on its first context and the
-    choice applied to every context of that shape.  Returns the choices in item
-    order; `cache` (a dict) carries choices across calls."""
-    cache = {} if cache is None else cache
-    out = []
-    for asm, op, key in items:
-        if key not in cache:
-            cache[key] = tune(asm, op, "fp32", repeats=repeats, device=device,
-                              kernels=(1,))["choice"]
-        _apply(asm, cache[key])
-        out.append(cache[key])
-    return out
+BATCH_TILE_CANDIDATES = [(40, 448), (48, 512), (48, 544), (56, 576)]
+
+
+def tune_batch(items, repeats: int = 3, device: int = 0,
+               candidates=BATCH_TILE_CANDIDATES) -> dict:
+    """One FP32 tile size (rows, elements) for every mesh of a batch: the batch's
+    persistent kernel lays its shared memory out for the largest tile of any of
+    its meshes, so a size that suits one mesh alone can cost every other tile an
+    SM slot; the candidates are therefore timed on the whole batch.  `items` are
+    (Assembler, op, coefSets) as Batch.add takes them; for each candidate the size
+    is applied to every context, a batch is built and its FP32 replay timed (host
+    wall time around replay + synchronise, median of `repeats` after one
+    warm-up).  Applies the fastest to the contexts and returns {"choice",
+    "timings"}; the caller builds its batch afterwards."""
+    import time
+    from .api import Batch
+    timings = []
+    for rows, elems in candidates:
+        for asm, _, _ in items:
+            asm.set_option("fp32_kernel", 1)
+            asm.set_option("tile_rows", rows)
+            asm.set_option("tile_elems", elems)
+        b = Batch(device)
+        try:
+            for asm, op, cs in items:
+                b.add(asm, op, cs)
+            b.assemble("fp32", prec=True)
+            b.synchronize()
+            ts = []
+            for _ in range(repeats):
+                t0 = time.perf_counter()
+                b.assemble("fp32", prec=True)
+                b.synchronize()
+                ts.append(time.perf_counter() - t0)
+            timings.append(({"fp32_kernel": 1, "tile_rows": rows, "tile_elems": elems},
+                            statistics.median(ts) * 1e3))
+        except Exception:
+            continue   # a tile that cannot hold one row's elements
+        finally:
+            b.close()
+    choice, ms = min(timings, key=lambda x: x[1])
+    for asm, _, _ in items:
+        _apply(asm, choice)
+    return {"choice": choice, "ms": ms, "timings": [[c, t] for c, t in timings]}
 
 
 RENUMBERINGS = ("identity", "rcm", "morton", "bisection")

@@ -29,9 +29,9 @@ def test_tuned_batch_fp64_bit_exact_and_fp32_within_tolerance(gpu):
         a.set_coefficients(op, m.coef)
         cs = np.stack([mm.coef for mm in meshes])
         items.append((a, op, m, cs, row, col))
-        pending.append((a, op, (op, n)))
-    choices = autotune.tune_batch_items(pending, repeats=1)
-    assert all(c["fp32_kernel"] == 1 and c["tile_elems"] >= 64 for c in choices)
+        pending.append((a, op, cs))
+    tuned = autotune.tune_batch(pending, repeats=1)
+    assert tuned["choice"]["fp32_kernel"] == 1 and len(tuned["timings"]) >= 2
     for a, op, m, cs, _, _ in items:
         b.add(a, op, cs)
     b.assemble("fp64", prec=True)
