@@ -55,9 +55,11 @@ def test_fullsize_lap_symmetry_and_row_sums(gpu, mesh):
 
 def test_fullsize_fp32_within_tolerance_and_batch_equal(gpu, mesh):
     """FP32 tile path at full size against the FP64 assembly (bit-identical to the
-    oracle, above): max entry error below 2e-6 of the diagonal scale, Frobenius
-    and preconditioned-operator errors below 1e-6; the batched form with one
-    coefficient set gives the same bits as the single-mesh launch."""
+    oracle, above): max entry error below 1e-6 of the diagonal scale (the raw
+    relative error per value is reported beside it: below 3e-6 over the values
+    at least 0.1 of their diagonal scale), Frobenius and preconditioned-operator
+    errors below 1e-6; the batched form with one coefficient set gives the same
+    bits as the single-mesh launch."""
     import minifem
     from minifem import metrics
     a = gpu(0)
@@ -70,7 +72,8 @@ def test_fullsize_fp32_within_tolerance_and_batch_equal(gpu, mesh):
     a.assembly("ela", "fp32", "gather", prec=True)
     v32, p32 = a.values_f32(), a.prec()
     err = metrics.entry_errors(row, col, v64, v32, 9)
-    assert err["max_rel_diag_scaled"] < 2e-6, err
+    assert err["max_rel_diag_scaled"] < 1e-6, err
+    assert err["raw"]["tau_0.1"]["max"] < 3e-6, err
     assert err["frobenius_rel"] < 1e-6, err
     assert metrics.operator_error(row, col, v64, p64, v32, p32, 9) < 1e-6
     b = minifem.Batch(0)
