@@ -183,8 +183,9 @@ void adopt_pattern(Context &c, const int *hRow, const int *hCol, int nnz);
 void build_elem_pos(Context &c);
 void build_gather_plan(Context &c);
 
-// tiles.cu
+// tiles.cu, tileplan.cu
 void build_tile_plan(Context &c);
+void build_tile_plan_device(Context &c);
 void assemble_tiles32(Context &c, int op, bool fusePrec);
 void split_and_weights(Context &c, int op, float4 *hl, float2 *w);
 TilePlanView plan_view(const TilePlan &tp);

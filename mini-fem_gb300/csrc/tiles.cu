@@ -25,15 +25,11 @@
 //      compensation and writes the 3x3 block (or scalar) to the CSR values;
 //      warps take 32 entries at a time from a shared counter, so that the warps
 //      of 3a and 3b join when their work is done.
-// The plan is built once per mesh on the host from the device pattern.  Every
-// contribution list is in ascending element order and every combination order
-// is fixed, so results are deterministic.
+// The plan is built once per mesh and pattern on the device (tileplan.cu).
+// Every contribution list is in node -> element incidence order and every
+// combination order is fixed, so results are deterministic.
 #include <algorithm>
-#include <atomic>
 #include <cstdint>
-#include <exception>
-#include <numeric>
-#include <thread>
 #include <vector>
 
 #include "context.h"
@@ -97,24 +93,7 @@ __global__ void k_split_and_weights(const double *__restrict__ coord, int nbNode
     }
 }
 
-uint32_t spread3(uint32_t v) {   // 10 bits -> every third bit
-    v &= 0x3ff;
-    v = (v | (v << 16)) & 0x030000FF;
-    v = (v | (v << 8)) & 0x0300F00F;
-    v = (v | (v << 4)) & 0x030C30C3;
-    v = (v | (v << 2)) & 0x09249249;
-    return v;
-}
-
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
-
-// Contribution code: local element l, and the gradient slots of its nodes j and
-// k as the tile kernel lays them out (slot of node j = (j + l / 2) mod 4, see
-// gslot), so that the kernel finds gradient j at slot index code >> 2.
-unsigned short contrib_code(int l, int j, int k) {
-    const int r = l >> 1;
-    return (unsigned short)((l << 4) | (((j + r) & 3) << 2) | ((k + r) & 3));
-}
 
 }  // namespace
 
@@ -133,11 +112,6 @@ SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRow
     return L;
 }
 
-// Host-side plan construction (once per mesh and pattern).
-namespace {
-void build_tile_plan_impl(Context &c);
-}
-
 // A mesh the tiles cannot hold (a node touching more elements than a tile,
 // an entry with more than 255 contributions, a layout beyond shared memory) is
 // marked unfit: the FP32 path then uses the record kernel, which has no such
@@ -147,7 +121,7 @@ void build_tile_plan(Context &c) {
     if (tp.built) return;
     tp.unfit = false;
     try {
-        build_tile_plan_impl(c);
+        build_tile_plan_device(c);
     } catch (const Error &e) {
         if (e.code != MFEM_ERR_CAPACITY) throw;
         tp.unfit = true;
@@ -155,284 +129,6 @@ void build_tile_plan(Context &c) {
     }
 }
 
-namespace {
-
-// The plan is built in three passes: the rows in Morton order are cut into
-// tiles (sequential: a tile grows while its rows' elements fit), every tile's
-// lists are then built independently on all host threads, and the per-tile
-// lists are finally laid end to end with the padding the bulk copies need.
-struct TileLists {
-    std::vector<int> elems, nodes;
-    std::vector<ushort4> lconn;
-    std::vector<unsigned short> contrib;
-    std::vector<int2> diag;
-    std::vector<int4> off;
-};
-
-void build_tile_plan_impl(Context &c) {
-    TilePlan &tp = c.tiles;
-    build_incidence(c);
-    const int N = c.nbNodes, E = c.nbElem, nnz = c.nnz;
-    std::vector<double> coord((size_t)N * 3);
-    std::vector<int> e2n((size_t)E * 4), nptr(N + 1), nelem((size_t)E * 4), rowPtr(N + 1),
-        col((size_t)nnz);
-    MFEM_CUDA(cudaMemcpyAsync(coord.data(), c.coord.ptr, coord.size() * 8, cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaMemcpyAsync(e2n.data(), c.e2n.ptr, e2n.size() * 4, cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaMemcpyAsync(nptr.data(), c.nodeElemPtr.ptr, nptr.size() * 4, cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaMemcpyAsync(nelem.data(), c.nodeElem.ptr, nelem.size() * 4, cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaMemcpyAsync(rowPtr.data(), c.rowPtr.ptr, rowPtr.size() * 4, cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaMemcpyAsync(col.data(), c.col.ptr, col.size() * 4, cudaMemcpyDeviceToHost, c.stream));
-    MFEM_CUDA(cudaStreamSynchronize(c.stream));
-
-    // Morton order of the nodes (10 bits per axis over the bounding box)
-    double lo3[3] = {1e300, 1e300, 1e300}, hi3[3] = {-1e300, -1e300, -1e300};
-    for (int i = 0; i < N; i++)
-        for (int d = 0; d < 3; d++) {
-            lo3[d] = std::min(lo3[d], coord[3 * (size_t)i + d]);
-            hi3[d] = std::max(hi3[d], coord[3 * (size_t)i + d]);
-        }
-    std::vector<uint64_t> key(N);
-    for (int i = 0; i < N; i++) {
-        uint32_t q[3];
-        for (int d = 0; d < 3; d++) {
-            const double span = hi3[d] > lo3[d] ? hi3[d] - lo3[d] : 1.0;
-            const double f = (coord[3 * (size_t)i + d] - lo3[d]) / span;
-            q[d] = (uint32_t)std::min(1023.0, std::max(0.0, f * 1023.0));
-        }
-        const uint64_t m = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
-        key[i] = (m << 32) | (uint32_t)i;
-    }
-    std::sort(key.begin(), key.end());
-
-    // 1. the cut: consecutive rows while the tile's incident elements fit
-    std::vector<int> tileRowBegin, rowOrder(N), rowTile(N, -1), rowLocal(N, 0), mark(E, -1);
-    {
-        int i = 0, elemCount = 0;
-        while (i < N) {
-            const int t = (int)tileRowBegin.size();
-            tileRowBegin.push_back(i);
-            elemCount = 0;
-            int nr = 0;
-            while (i < N && nr < tp.maxRows) {
-                const int r = (int)(key[i] & 0xffffffffu);
-                int add = 0;
-                for (int q = nptr[r]; q < nptr[r + 1]; q++)
-                    if (mark[nelem[q] >> 2] != t) add++;
-                if (nr > 0 && elemCount + add > tp.maxElem) break;
-                MFEM_REQUIRE(elemCount + add <= tp.maxElem, MFEM_ERR_CAPACITY,
-                             "tile plan: one row touches more elements than a tile holds");
-                for (int q = nptr[r]; q < nptr[r + 1]; q++) mark[nelem[q] >> 2] = t;
-                elemCount += add;
-                rowOrder[i] = r;
-                rowTile[r] = t;
-                rowLocal[r] = nr++;
-                i++;
-            }
-        }
-        tileRowBegin.push_back(N);
-    }
-    MFEM_REQUIRE(tp.maxElem <= 4096, MFEM_ERR_CAPACITY, "tile plan: local index overflow");
-    const int nTiles = (int)tileRowBegin.size() - 1;
-
-    // 2. every tile's lists, tiles spread over the host threads
-    std::vector<TileLists> lists(nTiles);
-    auto buildTile = [&](int t, std::vector<int> &posInRow) {
-        TileLists &L = lists[t];
-        const int r0 = tileRowBegin[t], nRows = tileRowBegin[t + 1] - r0;
-        for (int lr = 0; lr < nRows; lr++) {
-            const int r = rowOrder[r0 + lr];
-            for (int q = nptr[r]; q < nptr[r + 1]; q++) L.elems.push_back(nelem[q] >> 2);
-        }
-        std::sort(L.elems.begin(), L.elems.end());
-        L.elems.erase(std::unique(L.elems.begin(), L.elems.end()), L.elems.end());
-        for (int e : L.elems)
-            for (int k = 0; k < 4; k++) L.nodes.push_back(e2n[4 * (size_t)e + k]);
-        std::sort(L.nodes.begin(), L.nodes.end());
-        L.nodes.erase(std::unique(L.nodes.begin(), L.nodes.end()), L.nodes.end());
-        auto nodeLocal = [&](int n) {
-            return (unsigned short)(std::lower_bound(L.nodes.begin(), L.nodes.end(), n) - L.nodes.begin());
-        };
-        auto elemLocal = [&](int e) {
-            return (int)(std::lower_bound(L.elems.begin(), L.elems.end(), e) - L.elems.begin());
-        };
-        L.lconn.reserve(L.elems.size());
-        for (int e : L.elems) {
-            const size_t b4 = 4 * (size_t)e;
-            L.lconn.push_back(make_ushort4(nodeLocal(e2n[b4]), nodeLocal(e2n[b4 + 1]),
-                                           nodeLocal(e2n[b4 + 2]), nodeLocal(e2n[b4 + 3])));
-        }
-        std::vector<int> cnt, start, fill;
-        std::vector<char> keep;
-        for (int lr = 0; lr < nRows; lr++) {
-            const int r = rowOrder[r0 + lr];
-            const int b = rowPtr[r], len = rowPtr[r + 1] - b;
-            // position of each column of row r in the row (node-indexed, reset below)
-            for (int m = 0; m < len; m++) posInRow[col[b + m]] = m;
-            // which entries of the row this tile computes: the diagonal, entries to
-            // rows outside the tile, and (r, c) with c a later row of the tile,
-            // which also yields (c, r) transposed
-            keep.assign(len, 0);
-            for (int m = 0; m < len; m++) {
-                const int cc = col[b + m];
-                keep[m] = cc == r || rowTile[cc] != t || rowLocal[cc] > lr;
-            }
-            cnt.assign(len, 0);
-            for (int q = nptr[r]; q < nptr[r + 1]; q++) {
-                const int e = nelem[q] >> 2;
-                for (int k = 0; k < 4; k++) {
-                    const int m = posInRow[e2n[4 * (size_t)e + k]];
-                    MFEM_REQUIRE(m >= 0, MFEM_ERR_PATTERN, "tile plan: pattern misses an element pair");
-                    cnt[m]++;
-                }
-            }
-            start.assign(len + 1, 0);
-            for (int m = 0; m < len; m++) start[m + 1] = start[m] + (keep[m] ? cnt[m] : 0);
-            const int base = (int)L.contrib.size();
-            L.contrib.resize(L.contrib.size() + start[len]);
-            fill.assign(len, 0);
-            for (int q = nptr[r]; q < nptr[r + 1]; q++) {
-                const int e = nelem[q] >> 2, j = nelem[q] & 3;
-                for (int k = 0; k < 4; k++) {
-                    const int m = posInRow[e2n[4 * (size_t)e + k]];
-                    if (!keep[m]) continue;
-                    L.contrib[base + start[m] + fill[m]++] = contrib_code(elemLocal(e), j, k);
-                }
-            }
-            bool hasDiag = false;
-            for (int m = 0; m < len; m++) {
-                if (!keep[m]) continue;
-                MFEM_REQUIRE(cnt[m] <= 255 && base + start[m] < (1 << 23), MFEM_ERR_CAPACITY,
-                             "tile plan: too many contributions for one entry");
-                const int meta = ((base + start[m]) << 8) | cnt[m];
-                const int cc = col[b + m];
-                if (cc == r) {
-                    L.diag.push_back(make_int2(r, meta));
-                    hasDiag = true;
-                } else {
-                    int tpos = -1;
-                    if (rowTile[cc] == t) {
-                        const int cb = rowPtr[cc], clen = rowPtr[cc + 1] - cb;
-                        for (int mm = 0; mm < clen; mm++)
-                            if (col[cb + mm] == r) { tpos = cb + mm; break; }
-                        MFEM_REQUIRE(tpos >= 0, MFEM_ERR_PATTERN, "tile plan: pattern is not symmetric");
-                    }
-                    L.off.push_back(make_int4(b + m, tpos, meta, 0));
-                }
-            }
-            if (!hasDiag) L.diag.push_back(make_int2(r, 0));
-            for (int m = 0; m < len; m++) posInRow[col[b + m]] = -1;
-        }
-    };
-    {
-        const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-        const int nThreads = (int)std::min<long long>(hw, std::max(1, nTiles / 16));
-        std::atomic<int> nextTile(0);
-        std::vector<std::exception_ptr> errs(nThreads);
-        auto worker = [&](int w) {
-            try {
-                std::vector<int> posInRow(N, -1);
-                for (int t; (t = nextTile.fetch_add(1)) < nTiles;) buildTile(t, posInRow);
-            } catch (...) {
-                errs[w] = std::current_exception();
-                nextTile.store(nTiles);
-            }
-        };
-        std::vector<std::thread> pool;
-        for (int w = 1; w < nThreads; w++) pool.emplace_back(worker, w);
-        worker(0);
-        for (auto &th : pool) th.join();
-        for (auto &e : errs)
-            if (e) std::rethrow_exception(e);
-    }
-
-    // 3. the lists end to end; every segment starts 16-byte aligned and is padded
-    // to whole 16-byte units that lie inside the arrays (one bulk copy each)
-    std::vector<TileDesc> tiles(nTiles);
-    size_t nE = 0, nN = 0, nC = 0, nD = 0, nO = 0;
-    for (const TileLists &L : lists) {
-        nE += L.elems.size();
-        nN += L.nodes.size();
-        nC += L.contrib.size() + 8;
-        nD += L.diag.size() + 1;
-        nO += L.off.size();
-    }
-    std::vector<int> tileElems, tileNodes;
-    std::vector<ushort4> lconn;
-    std::vector<unsigned short> contrib;
-    std::vector<int2> diagEnt;
-    std::vector<int4> offEnt;
-    tileElems.reserve(nE);
-    lconn.reserve(nE);
-    tileNodes.reserve(nN);
-    contrib.reserve(nC);
-    diagEnt.reserve(nD);
-    offEnt.reserve(nO);
-    int maxElem = 0, maxContrib = 0, maxOff = 0, maxRows = 0, maxNodes = 0;
-    for (int t = 0; t < nTiles; t++) {
-        TileLists &L = lists[t];
-        TileDesc &T = tiles[t];
-        T.elemBegin = (int)tileElems.size();
-        T.nElem = (int)L.elems.size();
-        tileElems.insert(tileElems.end(), L.elems.begin(), L.elems.end());
-        lconn.insert(lconn.end(), L.lconn.begin(), L.lconn.end());
-        T.nodeBegin = (int)tileNodes.size();
-        T.nNodes = (int)L.nodes.size();
-        tileNodes.insert(tileNodes.end(), L.nodes.begin(), L.nodes.end());
-        T.offBegin = (int)offEnt.size();
-        T.diagBegin = (int)diagEnt.size();
-        T.contribBegin = (int)contrib.size();
-        T.nRows = tileRowBegin[t + 1] - tileRowBegin[t];
-        offEnt.insert(offEnt.end(), L.off.begin(), L.off.end());
-        diagEnt.insert(diagEnt.end(), L.diag.begin(), L.diag.end());
-        contrib.insert(contrib.end(), L.contrib.begin(), L.contrib.end());
-        T.nOff = (int)L.off.size();
-        T.nContrib = (int)L.contrib.size();
-        while (diagEnt.size() % 2) diagEnt.push_back(make_int2(0, 0));
-        while (contrib.size() % 8) contrib.push_back(0);
-        T.nOffPad = (int)offEnt.size() - T.offBegin;
-        T.nRowsPad = (int)diagEnt.size() - T.diagBegin;
-        T.nContribPad = (int)contrib.size() - T.contribBegin;
-        maxElem = std::max(maxElem, T.nElem);
-        maxContrib = std::max(maxContrib, T.nContribPad);
-        maxOff = std::max(maxOff, T.nOffPad);
-        maxRows = std::max(maxRows, T.nRowsPad);
-        maxNodes = std::max(maxNodes, T.nNodes);
-        L = TileLists();   // release as we go
-    }
-
-    tp.nTiles = (int)tiles.size();
-    tp.layout = smem_layout(std::max(maxElem, 1), maxContrib, maxOff, maxRows, maxNodes);
-    tp.planMax[0] = std::max(maxElem, 1);
-    tp.planMax[1] = maxContrib;
-    tp.planMax[2] = maxOff;
-    tp.planMax[3] = maxRows;
-    tp.planMax[4] = maxNodes;
-    MFEM_REQUIRE(tp.layout.bytes <= 227 * 1024, MFEM_ERR_CAPACITY,
-                 "tile plan: a tile needs more than 227 KB of shared memory");
-    auto up = [&](DevBuf &d, const void *src, size_t bytes) {
-        d.reserve(std::max<size_t>(bytes, 16));
-        if (bytes) MFEM_CUDA(cudaMemcpyAsync(d.ptr, src, bytes, cudaMemcpyHostToDevice, c.stream));
-    };
-    up(tp.desc, tiles.data(), tiles.size() * sizeof(TileDesc));
-    up(tp.elems, tileElems.data(), tileElems.size() * 4);
-    up(tp.lconn, lconn.data(), lconn.size() * sizeof(ushort4));
-    up(tp.nodes, tileNodes.data(), tileNodes.size() * 4);
-    up(tp.offEnt, offEnt.data(), offEnt.size() * sizeof(int4));
-    up(tp.diagEnt, diagEnt.data(), diagEnt.size() * sizeof(int2));
-    up(tp.contrib, contrib.data(), contrib.size() * 2);
-    MFEM_CUDA(cudaStreamSynchronize(c.stream));
-    tp.nTileElems = 0;
-    tp.nUnits = 0;
-    tp.nContrib = 0;
-    for (const TileDesc &T : tiles) {
-        tp.nTileElems += T.nElem;
-        tp.nUnits += T.nOff;
-        tp.nContrib += T.nContrib;
-    }
-    tp.built = true;
-}
-
-}  // namespace
 
 TilePlanView plan_view(const TilePlan &tp) {
     TilePlanView P;
