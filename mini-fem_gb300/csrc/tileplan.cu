@@ -684,7 +684,8 @@ void build_tile_plan_device(Context &c) {
                  "tile plan: a tile needs more than 227 KB of shared memory");
 
     // filling pass
-    auto alloc = [](DevBuf &d, size_t bytes) { return d.reserve(std::max<size_t>(bytes, 16)); };
+    // 16 bytes of slack: the tile kernel's L2 prefetches widen segments to 16-byte boundaries
+    auto alloc = [](DevBuf &d, size_t bytes) { return d.reserve(bytes + 16); };
     TileDesc *desc = (TileDesc *)alloc(tp.desc, tiles.size() * sizeof(TileDesc));
     MFEM_CUDA(cudaMemcpyAsync(desc, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, st));
     D.desc = desc;

@@ -2,7 +2,10 @@
 //
 // The rows (nodes) are put in Morton order of their coordinates and cut into
 // tiles of at most maxRows rows whose incident elements number at most maxElem.
-// One CTA per tile:
+// One CTA per tile (about four per SM):
+//   -. one thread prefetches into L2 (cp.async.bulk.prefetch) the plan
+//      segments of the tile that starts about one wave later, when this CTA's
+//      slot frees (blockIdx + 4 x SMs); CTA 0 prefetches every tile descriptor;
 //   0. one thread starts TMA bulk copies (cp.async.bulk, completion on an
 //      mbarrier) of the tile's contribution lists and diagonal table;
 //   1. meanwhile the CTA gathers the coordinates of the tile's nodes (one
@@ -41,11 +44,36 @@ namespace mfem {
 
 namespace {
 
+// L2 prefetch of [base + off, + len) widened to 16-byte boundaries (the plan
+// arrays are allocated with 16 bytes of slack, so the range stays inside them)
+__device__ __forceinline__ void prefetch_range(const void *base, size_t off, size_t len) {
+    if (!len) return;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(base) + off, b = a + len;
+    const uintptr_t a16 = a & ~(uintptr_t)15, b16 = (b + 15) & ~(uintptr_t)15;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a16), "r"((unsigned)(b16 - a16))
+                 : "memory");
+}
+
 template <int OP, bool PREC>
 __global__ void __launch_bounds__(kTileThreads, 4)
 k_tile32(TilePlanView P, TileMesh M, TileSets S, SmemLayout L, float qthr2, int *counters,
          TileCtl ctl) {
     extern __shared__ __align__(16) unsigned char sm[];
+    if (threadIdx.x == 32) {
+        // the descriptors of every tile, then the plan segments of the tile that
+        // starts about one wave later (when this CTA's slot frees), into L2
+        if (blockIdx.x == 0) prefetch_range(P.desc, 0, (size_t)ctl.nTiles * sizeof(TileDesc));
+        const int nt = (int)blockIdx.x + ctl.pfDist;
+        if (ctl.pfDist > 0 && nt < ctl.nTiles) {
+            const TileDesc N = P.desc[nt];
+            prefetch_range(P.contrib, (size_t)N.contribBegin * 2, (size_t)N.nContribPad * 2);
+            prefetch_range(P.diagEnt, (size_t)N.diagBegin * 8, (size_t)N.nRowsPad * 8);
+            prefetch_range(P.offEnt, (size_t)N.offBegin * 16, (size_t)N.nOffPad * 16);
+            prefetch_range(P.lconn, (size_t)N.elemBegin * 8, (size_t)N.nElem * 8);
+            prefetch_range(P.elems, (size_t)N.elemBegin * 4, (size_t)N.nElem * 4);
+            prefetch_range(P.nodes, (size_t)N.nodeBegin * 4, (size_t)N.nNodes * 4);
+        }
+    }
     const TileDesc T = P.desc[blockIdx.x];
     tilek::tile_body<OP, PREC>(T, M, S, P, L, qthr2, sm, counters, ctl);
 }
@@ -197,11 +225,14 @@ void assemble_tiles32(Context &c, int op, bool fusePrec) {
     const TilePlanView P = plan_view(tp);
     const SmemLayout L = tp.layout;
     const float q = c.sliverThreshold;
+    int sms = 0;
+    MFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
     c.timer.begin(fusePrec ? "tile32+prec" : "tile32", c.stream);
     auto launch = [&](auto kern) {
         MFEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
         kern<<<tp.nTiles, kTileThreads, L.bytes, c.stream>>>(P, M, S, L, q * q, st + 4,
-                                                             TileCtl{c.waitLimit, c.testExtraTx});
+                                                             TileCtl{c.waitLimit, c.testExtraTx, tp.nTiles,
+                                                                     4 * sms});
     };
     if (op == MFEM_OP_LAP) {
         if (fusePrec) launch(k_tile32<MFEM_OP_LAP, true>);

@@ -65,6 +65,8 @@ struct TileSets {
 struct TileCtl {
     unsigned waitLimit;
     unsigned extraTx;
+    int nTiles;      // single-mesh launch: tiles in the grid
+    int pfDist;      // prefetch into L2 the plan segments of tile blockIdx + pfDist (0: none)
 };
 
 // Byte offsets of the dynamic shared-memory regions.  The tile's node
