@@ -663,14 +663,17 @@ def _timer(torch, stream, flush):
     return run
 
 
-def run_cube30(args, op):
-    """30^3 cube (146,334 tets), lap or ela: FP64 gather (bit-exact), colour scatter,
-    atomics and FP32, with the oracle port timed beside them."""
+def run_cube30(args, op, side=30):
+    """side^3 cube (30^3: 146,334 tets), lap or ela: FP64 gather (bit-exact), colour
+    scatter, atomics and FP32, with the oracle port timed beside them; the scatter
+    and atomic results against the gather (max entry difference over the diagonal
+    scale)."""
     import torch
     import minifem
     import pyoracle as O
+    from minifem import metrics
     from minifem.meshgen import cube_mesh
-    mesh = cube_mesh(30, seed=SEED, op=op)
+    mesh = cube_mesh(side, seed=SEED, op=op)
     E, N = mesh.nbElem, mesh.nbNodes
     a = minifem.Assembler(0)
     a.set_mesh(mesh.coord, mesh.elemToNode)
@@ -682,10 +685,16 @@ def run_cube30(args, op):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
     timed = _timer(torch, torch.cuda.ExternalStream(a.stream), flush)
     res = {}
+    dim = 1 if op == "lap" else 9
+    a.assembly(op, "fp64", "gather", prec=True)
+    gathered = a.values()
     for name, prec, strat in (("fp64_gather", "fp64", "gather"), ("fp64_scatter", "fp64", "scatter"),
                               ("fp64_atomic", "fp64", "atomic"), ("fp32_tiles", "fp32", "gather")):
         ms = timed(lambda: a.assembly(op, prec, strat, prec=True), args.steps, args.warmup)
         res[name] = {"ms_per_step": round(ms, 4), "value": round(E / (ms * 1e-3) / 1e6, 1)}
+        if strat != "gather":
+            res[name]["max_rel_diag_scaled_vs_gather"] = metrics.entry_errors(
+                row, col, gathered, a.values(), dim)["max_rel_diag_scaled"]
     a.assembly(op, "fp64", "gather", prec=True)
     ref = O.full(mesh, op=op)
     bit_exact = (a.values().tobytes() == ref["values"].tobytes()
@@ -698,12 +707,12 @@ def run_cube30(args, op):
         O.prec(v, ref["row"], ref["col"], markf, N, op)
         t.append(time.perf_counter() - t0)
     cpu = E / statistics.mean(t) / 1e6
-    return {"metric": f"{op} assembly + preconditioner Melem/s @146k tets (FP64 gather)",
+    return {"metric": f"{op} assembly + preconditioner Melem/s @{E // 1000}k tets (FP64 gather)",
             "value": res["fp64_gather"]["value"], "unit": "Melem/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": res["fp64_gather"]["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{op}_cube30_146k_tets", "nbElem": E, "nbNodes": N,
+            "config": {"workload": f"{op}_cube{side}_{E // 1000}k_tets", "nbElem": E, "nbNodes": N,
                        "nbEdges": len(col), "colours": ncol},
             "variants": res, "bit_exact_vs_oracle": bit_exact,
             "cpu_baseline": {"value": round(cpu, 3), "unit": "Melem/s", "cores": 1, "kind": "port",
@@ -925,8 +934,8 @@ def main():
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--workload", default="ela100",
-                    choices=["ela100", "ela30", "lap30", "stress60", "batch64", "solve100",
-                             "renumber100"],
+                    choices=["ela100", "ela30", "lap30", "strategies100", "stress60", "batch64",
+                             "solve100", "renumber100"],
                     help="ela100: the benchmark line; the others: the remaining configurations")
     ap.add_argument("--side", type=int, default=N_SIDE,
                     help="nodes per cube side (100 = the benchmark mesh; smaller for profiling)")
@@ -953,6 +962,8 @@ def main():
             out = None
         elif args.workload in ("ela30", "lap30"):
             out = run_cube30(args, args.workload[:3])
+        elif args.workload == "strategies100":
+            out = run_cube30(args, "ela", side=100)
         elif args.workload == "stress60":
             out = run_stress(args)
         elif args.workload == "solve100":

@@ -555,7 +555,8 @@ void build_tile_plan_device(Context &c) {
     k_morton<<<blocks_for(N, kPlanThreads), kPlanThreads, 0, st>>>(c.coord.as<double>(), N, box, key, id);
     check_launch("k_morton");
     const int nSortBlocks = (N + kSortTile - 1) / kSortTile;
-    int *hist = (int *)dHist.reserve(sizeof(int) * 256 * (size_t)nSortBlocks);
+    // one more word: the scan writes its total after the last entry
+    int *hist = (int *)dHist.reserve(sizeof(int) * (256 * (size_t)nSortBlocks + 1));
     int *scanTmp = (int *)dScan.reserve(sizeof(int) * scan_tmp_elems(256LL * nSortBlocks));
     for (int shift = 0; shift < 30; shift += 8) {   // 30-bit keys
         k_radix_hist<<<nSortBlocks, kPlanThreads, 0, st>>>(key, N, shift, hist, nSortBlocks);

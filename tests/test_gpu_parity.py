@@ -134,9 +134,9 @@ def test_elem_to_edge_matches_reference(gpu):
 
 
 @pytest.mark.parametrize("strategy", ["scatter", "atomic"])
-@pytest.mark.parametrize("op", ["lap", "ela"])
-def test_reordered_fp64_strategies(gpu, strategy, op):
-    m = cube_mesh(12, seed=8, op=op)
+@pytest.mark.parametrize("op,n", [("lap", 12), ("ela", 12), ("ela", 30)])
+def test_reordered_fp64_strategies(gpu, strategy, op, n):
+    m = cube_mesh(n, seed=8, op=op)
     row, col, vals, prec = gpu_full(gpu, m, op, m.coef, "reference", strategy=strategy)
     ref = O.full(m, op=op)
     d = O.op_dim(op)
