@@ -56,16 +56,10 @@ __device__ __forceinline__ unsigned spread3(unsigned v) {   // 10 bits -> every 
     return v;
 }
 
-// Bounding box of the coordinates (one block): box = (lo x, y, z, hi x, y, z).
-__global__ void k_bbox(const double *__restrict__ coord, int N, double *__restrict__ box) {
-    __shared__ double s[6][32];
-    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-    for (int i = threadIdx.x; i < N; i += blockDim.x)
-        for (int d = 0; d < 3; d++) {
-            const double x = coord[3 * (size_t)i + d];
-            v[d] = fmin(v[d], x);
-            v[3 + d] = fmax(v[3 + d], x);
-        }
+// Bounding box of the coordinates in two launches: every block reduces a
+// grid-strided share of the nodes to part[6 * block] = (lo x, y, z, hi x, y, z),
+// then one block reduces the parts (nParts of them) to box[0..5].
+__device__ __forceinline__ void block_minmax6(double v[6], double *sRed /* [6][32] */) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int d = 0; d < 6; d++) {
         double x = v[d];
@@ -73,15 +67,37 @@ __global__ void k_bbox(const double *__restrict__ coord, int N, double *__restri
             const double y = __shfl_xor_sync(0xffffffffu, x, off);
             x = d < 3 ? fmin(x, y) : fmax(x, y);
         }
-        if (lane == 0) s[d][warp] = x;
+        if (lane == 0) sRed[d * 32 + warp] = x;
     }
     __syncthreads();
     if (threadIdx.x < 6) {
         const int d = threadIdx.x;
-        double x = s[d][0];
-        for (int w = 1; w < nw; w++) x = d < 3 ? fmin(x, s[d][w]) : fmax(x, s[d][w]);
-        box[d] = x;
+        double x = sRed[d * 32];
+        for (int w = 1; w < nw; w++) x = d < 3 ? fmin(x, sRed[d * 32 + w]) : fmax(x, sRed[d * 32 + w]);
+        v[d] = x;
     }
+}
+
+__global__ void k_bbox_part(const double *__restrict__ coord, int N, double *__restrict__ part) {
+    __shared__ double sRed[6 * 32];
+    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+        for (int d = 0; d < 3; d++) {
+            const double x = coord[3 * (size_t)i + d];
+            v[d] = fmin(v[d], x);
+            v[3 + d] = fmax(v[3 + d], x);
+        }
+    block_minmax6(v, sRed);
+    if (threadIdx.x < 6) part[6 * blockIdx.x + threadIdx.x] = v[threadIdx.x];
+}
+
+__global__ void k_bbox_final(const double *__restrict__ part, int nParts, double *__restrict__ box) {
+    __shared__ double sRed[6 * 32];
+    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int b = threadIdx.x; b < nParts; b += blockDim.x)
+        for (int d = 0; d < 6; d++) v[d] = d < 3 ? fmin(v[d], part[6 * b + d]) : fmax(v[d], part[6 * b + d]);
+    block_minmax6(v, sRed);
+    if (threadIdx.x < 6) box[threadIdx.x] = v[threadIdx.x];
 }
 
 // Morton key of every node (10 bits per axis over the box) and its id.
@@ -545,13 +561,17 @@ void build_tile_plan_device(Context &c) {
 
     // 1. Morton order of the nodes
     DevBuf dBox, dKey, dId, dKey2, dId2, dHist, dPos, dPrev, dEnd, dScan;
-    double *box = (double *)dBox.reserve(6 * sizeof(double));
+    const int nParts = (int)std::min<long long>(blocks_for(N, kPlanThreads), 4096);
+    double *box = (double *)dBox.reserve(6 * sizeof(double) * (size_t)(nParts + 1));
+    double *part = box + 6;
     unsigned *key = (unsigned *)dKey.reserve(sizeof(unsigned) * (size_t)N);
     unsigned *key2 = (unsigned *)dKey2.reserve(sizeof(unsigned) * (size_t)N);
     int *id = (int *)dId.reserve(sizeof(int) * (size_t)N);
     int *id2 = (int *)dId2.reserve(sizeof(int) * (size_t)N);
-    k_bbox<<<1, 1024, 0, st>>>(c.coord.as<double>(), N, box);
-    check_launch("k_bbox");
+    k_bbox_part<<<nParts, kPlanThreads, 0, st>>>(c.coord.as<double>(), N, part);
+    check_launch("k_bbox_part");
+    k_bbox_final<<<1, kPlanThreads, 0, st>>>(part, nParts, box);
+    check_launch("k_bbox_final");
     k_morton<<<blocks_for(N, kPlanThreads), kPlanThreads, 0, st>>>(c.coord.as<double>(), N, box, key, id);
     check_launch("k_morton");
     const int nSortBlocks = (N + kSortTile - 1) / kSortTile;
