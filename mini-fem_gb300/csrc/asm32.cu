@@ -1,7 +1,8 @@
 // FP32 assembly: element arithmetic and CSR values in FP32, every entry summed
 // with Kahan compensation, FP64 kept for the coordinate differences (through a
-// hi/lo float split of the coordinates), for elements flagged as slivers by a
-// quality test, and for the 3x3 diagonal-block inversion.
+// hi/lo float split of the coordinates) and for the 3x3 diagonal-block
+// inversion; elements flagged as slivers by a quality test get double-float
+// gradients (grad_df.cuh).
 //
 // Same structure as the FP64 gather (gradient records, then one thread per upper
 // CSR entry and its transpose); records are 64 bytes (12 gradient floats + the
@@ -9,6 +10,7 @@
 // the compensated sum (prec_init + prec_inversion fused).
 #include "context.h"
 #include "elem_math.cuh"
+#include "grad_df.cuh"
 
 namespace mfem {
 
@@ -76,12 +78,17 @@ k_grad32(const float4 *__restrict__ hi, const float4 *__restrict__ lo,
     const float nc = fmaf(xc, xc, fmaf(yc, yc, zc * zc));
     float4 *out = reinterpret_cast<float4 *>(rec + (size_t)e * kRec32);
     if (vol * vol < qthr2 * (na * nb) * nc) {
-        // sliver: FP64 Jacobian determinant and inverse
+        // sliver: double-float gradients from the same hi/lo coordinates
+        // (grad_df.cuh); a zero volume takes the FP64 formula and its infinities
         atomicAdd(flagged, 1);
-        double gd[12];
-        elem_gradients(coord, nd, gd);
+        const float hx[4][3] = {{h0.x, h0.y, h0.z}, {h1.x, h1.y, h1.z}, {h2.x, h2.y, h2.z}, {h3.x, h3.y, h3.z}};
+        const float lx[4][3] = {{l0.x, l0.y, l0.z}, {l1.x, l1.y, l1.z}, {l2.x, l2.y, l2.z}, {l3.x, l3.y, l3.z}};
+        if (!grad_df(hx, lx, g)) {
+            double gd[12];
+            elem_gradients(coord, nd, gd);
 #pragma unroll
-        for (int i = 0; i < 12; i++) g[i] = __double2float_rn(gd[i]);
+            for (int i = 0; i < 12; i++) g[i] = __double2float_rn(gd[i]);
+        }
     } else {
         g[9] = -((g[0] + g[3]) + g[6]);
         g[10] = -((g[1] + g[4]) + g[7]);

@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "elem32.cuh"
+#include "grad_df.cuh"
 #include "tiles.cuh"
 
 namespace mfem {
@@ -278,9 +279,10 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     __syncthreads();
 
     // 1b. gradients of the tile's elements; flagged elements are queued (after
-    //     the coordinates) and get their FP64 gradients in a second pass by
-    //     consecutive threads, so that the FP64 work is spread over full warps
-    //     instead of stalling every warp that holds one flagged element
+    //     the coordinates) and get their double-float gradients (grad_df.cuh)
+    //     in a second pass by consecutive threads, so that the extra work is
+    //     spread over full warps instead of stalling every warp that holds one
+    //     flagged element
     unsigned short *sFlag = reinterpret_cast<unsigned short *>(sm + L.q);
     for (int i = tid; i < T.nElem; i += kTileThreads) {
         const ushort4 lc = i == i0 ? lc0 : i == i1 ? lc1 : P.lconn[T.elemBegin + i];
@@ -300,8 +302,18 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         for (int k = tid; k < nFlagged; k += kTileThreads) {
             const int i = sFlag[k];
             const ushort4 lc = P.lconn[T.elemBegin + i];
-            float g[12];
-            grad32_fp64(M.coord, make_int4(nb[lc.x], nb[lc.y], nb[lc.z], nb[lc.w]), g);
+            const unsigned short ln[4] = {lc.x, lc.y, lc.z, lc.w};
+            float hi[4][3], lo[4][3], g[12];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float4 h = Xh[ln[j]], l = Xl[ln[j]];
+                hi[j][0] = h.x; hi[j][1] = h.y; hi[j][2] = h.z;
+                lo[j][0] = l.x; lo[j][1] = l.y; lo[j][2] = l.z;
+            }
+            // double-float from the staged coordinates; a zero volume takes the
+            // FP64 formula and its infinities
+            if (!grad_df(hi, lo, g))
+                grad32_fp64(M.coord, make_int4(nb[lc.x], nb[lc.y], nb[lc.z], nb[lc.w]), g);
 #pragma unroll
             for (int j = 0; j < 4; j++) G[gslot(i, j)] = make_float4(g[3 * j], g[3 * j + 1], g[3 * j + 2], 0.f);
         }
