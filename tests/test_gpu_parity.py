@@ -265,6 +265,22 @@ def test_isolated_node_and_singular_block(gpu):
         ref = O.full(M, op=op, coef=None)
         assert vals.tobytes() == ref["values"].tobytes()
         assert prec.tobytes() == ref["prec"].tobytes()
+        # the FP32 tile path: the isolated node is an empty row of the device
+        # tile plan; values within the FP32 tolerance, the preconditioner
+        # non-finite exactly where the reference's is and close elsewhere
+        a = gpu(0)
+        a.set_option("fp32_kernel", 1)
+        a.set_mesh(M.coord, M.elemToNode)
+        a.create_nodeToNode("reference")
+        a.set_coefficients(op, None)
+        a.set_check_bounds(O.checkbounds(M.boundNodesCode))
+        a.assembly(op, "fp32", "gather", prec=True)
+        v = a.values_f32().astype(np.float64)
+        assert np.abs(v - ref["values"]).max() <= TOL_FP32 * np.abs(ref["values"]).max()
+        p = a.prec()
+        fin = np.isfinite(ref["prec"])
+        assert np.array_equal(np.isfinite(p), fin)
+        assert np.abs(p[fin] - ref["prec"][fin]).max() <= 1e-4 * np.abs(ref["prec"][fin]).max()
 
 
 def test_empty_mesh_is_rejected(gpu):
