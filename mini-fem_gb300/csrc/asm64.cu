@@ -82,10 +82,27 @@ __device__ __forceinline__ double fix_zero(double x) {
     return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
 }
 
-template <int OP, bool COEF>
+// (A, B, mu) of every element from (E, nu), for the gradient kernel to read
+// instead of forming them (two correctly rounded divisions on the FP64 pipe)
+// every step; made once per coefficient upload.
+__global__ void __launch_bounds__(kThreads)
+k_lame64(const double *__restrict__ coef, int nbElem, double *__restrict__ lame) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nbElem) return;
+    double A, B, mu;
+    lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
+    lame[3 * (size_t)e] = A;
+    lame[3 * (size_t)e + 1] = B;
+    lame[3 * (size_t)e + 2] = mu;
+}
+
+// CACHED (ela with coefficients): the weights come from k_lame64's array, the
+// same bits as forming them here.
+template <int OP, bool COEF, bool CACHED = false>
 __global__ void __launch_bounds__(kThreads)
 k_grad64(const double *__restrict__ coord, const int4 *__restrict__ e2n,
-         const double *__restrict__ coef, int nbElem, double *__restrict__ rec) {
+         const double *__restrict__ coef, int nbElem, double *__restrict__ rec,
+         const double *__restrict__ lame = nullptr) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nbElem) return;
     double g[12];
@@ -97,7 +114,13 @@ k_grad64(const double *__restrict__ coord, const int4 *__restrict__ e2n,
         store_record(rec, e, g, kappa, kappa, kappa, kappa);
     } else {
         double A, B, mu;
-        lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
+        if (CACHED) {
+            A = lame[3 * (size_t)e];
+            B = lame[3 * (size_t)e + 1];
+            mu = lame[3 * (size_t)e + 2];
+        } else {
+            lame_weights(coef[2 * (size_t)e], coef[2 * (size_t)e + 1], A, B, mu);
+        }
         store_record(rec, e, g, A, B, mu, A);
     }
 }
@@ -370,9 +393,21 @@ void launch_gather(Context &c, bool fusePrec) {
     const GatherPlan &g = c.gather;
     const int E = c.nbElem, N = c.nbNodes;
     double *rec = (double *)c.grad.reserve(sizeof(double) * kRec64 * (size_t)E);
-    c.timer.begin("grad64", c.stream);
-    k_grad64<OP, COEF><<<blocks_for(E, kThreads), kThreads, 0, c.stream>>>(
-        c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(), E, rec);
+    if constexpr (OP == MFEM_OP_ELA && COEF) {
+        if (!c.lameValid) {
+            double *lame = (double *)c.lame.reserve(sizeof(double) * 3 * (size_t)E);
+            k_lame64<<<blocks_for(E, kThreads), kThreads, 0, c.stream>>>(c.coef.as<double>(), E, lame);
+            check_launch("k_lame64");
+            c.lameValid = true;
+        }
+        c.timer.begin("grad64", c.stream);
+        k_grad64<OP, COEF, true><<<blocks_for(E, kThreads), kThreads, 0, c.stream>>>(
+            c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(), E, rec, c.lame.as<double>());
+    } else {
+        c.timer.begin("grad64", c.stream);
+        k_grad64<OP, COEF><<<blocks_for(E, kThreads), kThreads, 0, c.stream>>>(
+            c.coord.as<double>(), c.e2n.as<int4>(), c.coef.as<double>(), E, rec);
+    }
     check_launch("k_grad64");
     c.timer.end(c.stream);
     const int dim = OP == MFEM_OP_LAP ? 1 : 9;
@@ -544,7 +579,7 @@ void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec,
         // the records' gradients depend on the mesh only: after the first set
         // of a mesh only the weights are rewritten (none at all for constants)
         if (!gradientsReady) {
-            grad<<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec);
+            grad<<<blocks_for(E, kThreads), kThreads, 0, s>>>(coord, e2n, coef, E, rec, nullptr);
         } else if (coef) {
             if (op == MFEM_OP_LAP) k_weights64<MFEM_OP_LAP><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coef, E, rec);
             else k_weights64<MFEM_OP_ELA><<<blocks_for(E, kThreads), kThreads, 0, s>>>(coef, E, rec);

@@ -132,6 +132,7 @@ void set_mesh(Context &c, const double *coord, const int *e2n, int nbElem, int n
     c.halo.built = false;
     c.precBlocks = false;
     c.coefOp = -1;
+    c.lameValid = false;
     c.hasMask = false;
     c.lastOp = -1;
     c.hostRow = c.hostCol = nullptr;
@@ -181,6 +182,7 @@ void upload_coords(Context &c, const double *coord) {
 void upload_coefficients(Context &c, int op, const double *coef) {
     require_mesh(c);
     MFEM_REQUIRE(op == MFEM_OP_LAP || op == MFEM_OP_ELA, MFEM_ERR_INVALID_ARG, "operatorID must be 0 or 1");
+    c.lameValid = false;
     if (!coef) {
         c.coefOp = -1;
         return;

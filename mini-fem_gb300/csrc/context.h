@@ -140,6 +140,8 @@ struct Context {
     // coefficients
     int coefOp = -1;                  // -1: reference constants
     DevBuf coef;                      // double [E] or [E*2]
+    DevBuf lame;                      // double [E*3]: (A, B, mu) of the ela coefficients
+    bool lameValid = false;           //   made from coef by the FP64 gather when stale
 
     // Dirichlet mask, one byte per node: bit k = DOF k constrained
     DevBuf mask;
