@@ -152,9 +152,9 @@ TRAFFIC_PER_ELEM = {"tile32+prec": (144.148992e6 + 94.183168e6) / 1232274,
 # (sm__thread_inst_executed_pipe_fp64_pred_on.sum / 1,232,274 tets;
 # profiles/fp64_pipe_ela_cube60.md).  Every count is a fixed number per element,
 # per contribution or per node, so it grows in proportion to the mesh.
-FP64_OPS_PER_ELEM = {"grad64": 73028928 / 1232274,
-                     "diag_units64+prec": 91198720 / 1232274,
-                     "edge_units64": 143159328 / 1232274}
+FP64_OPS_PER_ELEM = {"grad64": 42221856 / 1232274,
+                     "diag_units64+prec": 91199200 / 1232274,
+                     "edge_units64": 143159136 / 1232274}
 
 
 _MESHGEN = None
