@@ -816,7 +816,10 @@ def run_solve(args):
         wall = time.perf_counter() - t0
         out[prec] = {"spmv_ms": round(ms, 4), "spmv_GBs": round(byts / (ms * 1e-3) / 1e9, 1),
                      "spmv_hbm_frac": round(byts / (ms * 1e-3) / 1e9 / hbm, 4),
-                     "spmv_bytes": byts, "spmv_fp64_fma": 9 * nnz,
+                     "spmv_bytes": byts,
+                     "spmv_arithmetic": "FP64 FMA chain, 9 per block" if prec == "fp64" else
+                     "FP32 double-float (exact hi products, sums within a few 2^-48 of sum|a x|), "
+                     "x split into hi/lo FP32 by one extra pass inside the timed call",
                      "pcg_iterations": it, "pcg_relres": rel, "pcg_s": round(wall, 4),
                      "pcg_ms_per_iteration": round(wall * 1e3 / max(it, 1), 4)}
     return {"metric": "ela 100^3 operator apply GB/s and block-Jacobi PCG (consumer of the assembly)",

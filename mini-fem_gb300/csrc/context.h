@@ -168,6 +168,7 @@ struct Context {
     // scratch
     DevBuf grad;                      // per-element gradient records
     DevBuf solver;                    // CG work vectors (solve.cu)
+    DevBuf xsplit;                    // float2 [N*d]: hi/lo split of an SpMV operand (FP32 values)
     DevBuf scratch, scratch2, scanTmp;
     DevBuf status;                    // int[8] device-side error flags
     CachedGraph scatterGraph;         // the colour-ordered scatter (asm64.cu)

@@ -76,6 +76,17 @@ __device__ __forceinline__ float f64_to_f32(double x) {
     return __uint_as_float(r);
 }
 
+// x * 2^k, exact, by exponent arithmetic on the integer pipe when x and the
+// result are normal; otherwise (zero, subnormal, out of range) by a multiply.
+__device__ __forceinline__ double scale_pow2(double x, int k) {
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e > 0 && e + k > 0 && e + k < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
+    if (x == 0.0) return x;
+    const int kk = max(-1022, min(1023, k));
+    return x * __longlong_as_double((long long)(kk + 1023) << 52);
+}
+
 // float -> double is exact; done with integer operations so that it does not
 // occupy GB300's narrow FP64 pipe (zero and subnormal inputs take the
 // conversion instruction).

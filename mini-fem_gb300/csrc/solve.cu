@@ -17,6 +17,7 @@
 #include <cmath>
 
 #include "context.h"
+#include "dmul_int.cuh"
 #include "elem32.cuh"
 
 namespace mfem {
@@ -112,6 +113,260 @@ k_spmv(const int *__restrict__ rowPtr, const int *__restrict__ col, const V *__r
     if (partial) cta_sum(dot, partial);
 }
 
+// ---- FP32 values: the operator without the FP64 pipe ----
+//
+// x is scaled by the power of two 2^-kx that brings max |x| just below 1 (kx
+// from the largest |x| bit pattern, kept on the device in *xmax) and split into
+// FP32 hi + lo parts; every product a x_j is then the exact a hi (FP32 product
+// and its FMA error) plus the rounded a lo, summed in double-float, and y is
+// scaled back by 2^kx.
+
+// Largest |x| bit pattern (non-negative doubles order as their bit patterns)
+// of a CTA's values into *xmax: one atomic per CTA (every thread calls it).
+__device__ __forceinline__ void block_max_into(unsigned long long b, unsigned long long *xmax) {
+    __shared__ unsigned long long wm[kThreads / 32];
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, b, off);
+        b = o > b ? o : b;
+    }
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = wm[w] > b ? wm[w] : b;
+        if (b) atomicMax(xmax, b);
+    }
+}
+
+// grid of the grid-stride vector kernels that reduce a maximum: few enough
+// CTAs that their atomics on one word stay cheap
+constexpr long long kMaxCtas = 1024;
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
+// kx with 2^kx > max |x|; 0 for a zero or non-finite maximum.
+__device__ __forceinline__ int scale_exp(const unsigned long long *xmax) {
+    const int e = (int)(*xmax >> 52);
+    return (e == 0 || e == 0x7ff) ? 0 : e - 1022;
+}
+
+// hi + lo FP32 parts of x 2^-kx, on the integer pipes.  Zero gives (0, 0); a
+// value below 2^-60 max |x| (or subnormal) or a non-finite one gives a NaN hi
+// part, so that every row that reads it takes the FP64 path.
+__device__ __forceinline__ float2 split_x(double v, int kx) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    if ((b << 1) == 0u) return make_float2(0.f, 0.f);
+    const int e = (int)((b >> 52) & 0x7ffu);
+    uint32_t hb, lb;
+    if (e != 0x7ff && e - kx >= 1023 - 60 &&
+        split_f32_bits(b - ((unsigned long long)(long long)kx << 52), &hb, &lb))
+        return make_float2(__uint_as_float(hb), __uint_as_float(lb));
+    return make_float2(__int_as_float(0x7fffffff), 0.f);
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_xmax(const double *__restrict__ x, long long n, unsigned long long *__restrict__ xmax) {
+    unsigned long long b = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long v = abs_bits(x[i]);
+        b = v > b ? v : b;
+    }
+    block_max_into(b, xmax);
+}
+
+// The split of x, with the constrained DOFs (mask) as zero: the operator's
+// M x.
+template <int D>
+__global__ void k_split_x(const double *__restrict__ x, float2 *__restrict__ xs, long long n,
+                          const unsigned long long *__restrict__ xmax, const unsigned char *__restrict__ mask,
+                          const int *__restrict__ stop) {
+    if (stop && *stop) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool z = mask && constrained(mask, (int)(i / D), (int)(i % D), D);
+    xs[i] = z ? make_float2(0.f, 0.f) : split_x(x[i], scale_exp(xmax));
+}
+
+// asynchronous global -> shared copies (no register round trip): 4 bytes, and
+// 16 bytes (both addresses 16-byte aligned; L2 only, the values stream)
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+// k_spmv32: lanes per block row, and blocks of a row staged per lane and chunk
+constexpr int kLanes32 = 4;
+constexpr int kRows32 = kThreads / kLanes32;
+constexpr int kSpmvBlocksPerLane = 2;
+
+// y = A x for FP32 values from the split xs: the hi products by TwoSum into s,
+// every error term and lo product into t; the four lanes' (s, t) merged in
+// double-float; y = (s + t) 2^kx.  A lane's s + t is within a few 2^-48 of
+// sum |a x| of its blocks.
+//
+// Four lanes share a block row and take its blocks in chunks of 8 (lane l the
+// blocks l and l + 4): a chunk's values go to shared memory by 16-byte
+// asynchronous copies (from the 16-byte boundary at or below the chunk, the
+// last piece of the array by 4-byte copies) while its columns and x parts are
+// gathered.  The constrained columns are zero in xs already (k_split_x).
+//
+// A row whose largest |hi product| is outside [2^-60, 2^100] (overflow, values
+// near the FP32 underflow, an all-zero row, or an x entry that split_x marked)
+// or whose sums are not finite is recomputed by its lanes with k_spmv's FP64
+// chain on the unscaled x, in k_spmv's order and with its results.
+template <int D, bool DOT>
+__global__ void __launch_bounds__(kThreads)
+k_spmv32(const int *__restrict__ rowPtr, const int *__restrict__ col, const float *__restrict__ vals,
+         long long nVals, const float2 *__restrict__ xs, const unsigned long long *__restrict__ xmax,
+         const double *__restrict__ x, double *__restrict__ y, int N,
+         const unsigned char *__restrict__ mask, double *__restrict__ partial,
+         const int *__restrict__ stop) {
+    if (stop && *stop) return;
+    constexpr int B = D * D, BPL = kSpmvBlocksPerLane, CH = kLanes32 * BPL;
+    // a chunk's values from the 16-byte boundary at or below its start: at
+    // most 3 leading floats, whole 16-byte pieces
+    constexpr int kPieces = (3 + CH * B + 3) / 4, kRow = 4 * kPieces;
+    __shared__ __align__(16) float sv[kRows32][kRow];
+    const int g = threadIdx.x / kLanes32;
+    const int row = blockIdx.x * kRows32 + g;
+    const int sub = threadIdx.x % kLanes32;
+    const unsigned gmask = ((1u << kLanes32) - 1u) << (threadIdx.x & (32 - kLanes32));
+    const float *vend = vals + nVals;
+    float s[D], t[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) s[d] = t[d] = 0.f;
+    float pmax = 0.f;
+    int kb = 0, ke = 0;
+    if (row < N) {
+        kb = rowPtr[row];
+        ke = rowPtr[row + 1];
+    }
+    for (int k0 = kb; k0 < ke; k0 += CH) {
+        const int nb = min(CH, ke - k0);
+        int cc[BPL];
+#pragma unroll
+        for (int j = 0; j < BPL; j++) {
+            const int k = k0 + sub + kLanes32 * j;
+            cc[j] = k < ke ? col[k] : -1;
+        }
+        const float *cv = vals + (size_t)k0 * B;
+        const float *base = reinterpret_cast<const float *>(reinterpret_cast<uintptr_t>(cv) & ~(uintptr_t)15);
+        const int lead = (int)(cv - base);
+        const int np = (lead + nb * B + 3) >> 2;
+#pragma unroll
+        for (int r = 0; r < (kPieces + kLanes32 - 1) / kLanes32; r++) {
+            const int pc = sub + kLanes32 * r;
+            if (pc < np) {
+                const float *src = base + 4 * pc;
+                float *dst = &sv[g][4 * pc];
+                if (src + 4 <= vend) {
+                    cp_async16(dst, src);
+                } else {
+                    // the last piece of the array: only what lies inside it
+                    for (int q = 0; q < 4 && src + q < vend; q++) cp_async4(dst + q, src + q);
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        float2 xv[BPL][D];
+#pragma unroll
+        for (int j = 0; j < BPL; j++) {
+#pragma unroll
+            for (int d = 0; d < D; d++)
+                xv[j][d] = cc[j] >= 0 ? xs[(size_t)cc[j] * D + d] : make_float2(0.f, 0.f);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncwarp(gmask);
+#pragma unroll
+        for (int j = 0; j < BPL; j++) {
+            if (cc[j] < 0) continue;
+            const float *v = sv[g] + lead + (sub + kLanes32 * j) * B;
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+#pragma unroll
+                for (int jj = 0; jj < D; jj++) {
+                    const float a = v[D * i + jj];
+                    const float p = a * xv[j][jj].x;
+                    const float e = fmaf(a, xv[j][jj].x, -p);
+                    const float s1 = s[i] + p;
+                    const float bp = s1 - s[i];
+                    const float err = (s[i] - (s1 - bp)) + (p - bp);
+                    s[i] = s1;
+                    t[i] = fmaf(a, xv[j][jj].y, t[i]) + (e + err);
+                    pmax = fmaxf(pmax, fabsf(p));
+                }
+            }
+        }
+        __syncwarp(gmask);
+    }
+    // the row's four lanes: largest product, finiteness and the double-float
+    // sums, combined without the FP64 pipe
+    bool finite = true;
+#pragma unroll
+    for (int off = kLanes32 / 2; off >= 1; off >>= 1) {
+        pmax = fmaxf(pmax, __shfl_xor_sync(0xffffffffu, pmax, off));
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const float s2 = __shfl_xor_sync(0xffffffffu, s[d], off);
+            const float t2 = __shfl_xor_sync(0xffffffffu, t[d], off);
+            const float s1 = s[d] + s2;
+            const float bp = s1 - s[d];
+            const float err = (s[d] - (s1 - bp)) + (s2 - bp);
+            s[d] = s1;
+            t[d] = (t[d] + t2) + err;
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < D; d++) finite = finite && isfinite(s[d]) && isfinite(t[d]);
+    const bool bad = !(finite && pmax >= 0x1.0p-60f && pmax <= 0x1.0p100f);
+    double a[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) a[d] = 0.0;
+    if (__any_sync(0xffffffffu, bad)) {
+        if (bad) {
+            for (int k = kb + sub; k < ke; k += kLanes32) {
+                const int c = col[k];
+                const unsigned mc = mask ? mask[c] : 0u;
+                double xc[D];
+#pragma unroll
+                for (int d = 0; d < D; d++)
+                    xc[d] = (D == 1 ? mc != 0u : ((mc >> d) & 1u)) ? 0.0 : x[(size_t)c * D + d];
+                const float *v = vals + (size_t)k * B;
+#pragma unroll
+                for (int i = 0; i < D; i++)
+#pragma unroll
+                    for (int j = 0; j < D; j++) a[i] = fma(to_f64(v[D * i + j]), xc[j], a[i]);
+            }
+        }
+#pragma unroll
+        for (int off = kLanes32 / 2; off >= 1; off >>= 1)
+#pragma unroll
+            for (int d = 0; d < D; d++) a[d] += __shfl_xor_sync(0xffffffffu, a[d], off);
+    }
+    double dot = 0.0;
+    if (row < N && sub == 0) {
+        const int kx = scale_exp(xmax);
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const double xv = x[(size_t)row * D + d];
+            double yv = a[d];
+            if (!bad) yv = scale_pow2(f32_to_f64(s[d]) + f32_to_f64(t[d]), kx);
+            if (constrained(mask, row, d, D)) yv = xv;
+            y[(size_t)row * D + d] = yv;
+            if (DOT) dot = fma(xv, yv, dot);
+        }
+    }
+    if (DOT) cta_sum(dot, partial);
+}
+
 // z = P r (block-Jacobi), one thread per node.
 template <int D>
 __global__ void k_prec_apply(const double *__restrict__ prec, const double *__restrict__ r,
@@ -138,8 +393,9 @@ struct CgScalars {
 template <int D>
 __global__ void __launch_bounds__(kThreads)
 k_cg_init(const double *__restrict__ prec, const double *__restrict__ b, const double *__restrict__ q,
-          double *__restrict__ r, double *__restrict__ z, double *__restrict__ p, int N,
-          double *__restrict__ partial, int nCta) {
+          double *__restrict__ r, double *__restrict__ z, double *__restrict__ p,
+          unsigned long long *__restrict__ pmax, int N, double *__restrict__ partial, int nCta) {
+    unsigned long long pm = 0;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rz = 0.0, rr = 0.0, bb = 0.0;
     if (i < N) {
@@ -160,9 +416,12 @@ k_cg_init(const double *__restrict__ prec, const double *__restrict__ b, const d
             for (int c = 0; c < D; c++) s = fma(P[D * a + c], rv[c], s);
             z[(size_t)i * D + a] = s;
             p[(size_t)i * D + a] = s;
+            const unsigned long long sb = abs_bits(s);
+            pm = sb > pm ? sb : pm;
             rz = fma(rv[a], s, rz);
         }
     }
+    if (pmax) block_max_into(pm, pmax);
     cta_sum(rz, partial);
     __syncthreads();
     cta_sum(rr, partial + nCta);
@@ -241,8 +500,9 @@ k_cg_update(const double *__restrict__ prec, const CgScalars *__restrict__ sc,
     cta_sum(rr, partial + nCta);
 }
 
-__global__ void k_cg_beta(CgScalars *sc, const double *sums) {
+__global__ void k_cg_beta(CgScalars *sc, const double *sums, unsigned long long *pmax) {
     if (sc->stop) return;
+    if (pmax) *pmax = 0;
     const double rzNew = sums[0];
     sc->beta = sc->rz != 0.0 ? rzNew / sc->rz : 0.0;
     sc->rz = rzNew;
@@ -251,31 +511,67 @@ __global__ void k_cg_beta(CgScalars *sc, const double *sums) {
     if (sc->rr <= sc->tol2 * sc->bb || sc->iter >= sc->maxIter) sc->stop = 1;
 }
 
-// p = z + beta p
-__global__ void k_cg_direction(const CgScalars *__restrict__ sc, const double *__restrict__ z,
-                               double *__restrict__ p, long long n) {
+// p = z + beta p (and, for the FP32-valued operator, max |p| into *pmax,
+// which k_cg_beta cleared); grid-stride
+__global__ void __launch_bounds__(kThreads)
+k_cg_direction(const CgScalars *__restrict__ sc, const double *__restrict__ z,
+               double *__restrict__ p, unsigned long long *__restrict__ pmax, long long n) {
     if (sc->stop) return;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = fma(sc->beta, p[i], z[i]);
+    const double beta = sc->beta;
+    unsigned long long pm = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = fma(beta, p[i], z[i]);
+        p[i] = v;
+        const unsigned long long b = abs_bits(v);
+        pm = b > pm ? b : pm;
+    }
+    if (pmax) block_max_into(pm, pmax);
 }
 
+// Split of an SpMV operand for FP32 values: its hi/lo parts and the largest
+// |x| bit pattern that sets their scale.
+struct XSplit {
+    float2 *xs = nullptr;
+    unsigned long long *xmax = nullptr;
+};
+
+// FP32 values: the split of x made here (into c.xsplit) unless given with its
+// maximum already in xsp.xmax (the CG direction).
 template <int D>
-void spmv_t(const Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
-            const int *stop, cudaStream_t s) {
+void spmv_t(Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
+            const int *stop, XSplit xsp, cudaStream_t s) {
     const unsigned grid = blocks_for(c.nbNodes, kRowsPerCta);
-    if (c.lastPrecision == MFEM_FP32)
-        k_spmv<float, D><<<grid, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<float>(),
-                                                   x, y, c.nbNodes, mask, partial, stop);
-    else
+    if (c.lastPrecision == MFEM_FP32) {
+        const unsigned grid32 = blocks_for(c.nbNodes, kRows32);
+        const long long n = (long long)c.nbNodes * D;
+        if (!xsp.xs) {
+            char *w = (char *)c.xsplit.reserve(sizeof(float2) * (size_t)n + 256);
+            xsp.xmax = reinterpret_cast<unsigned long long *>(w);
+            xsp.xs = reinterpret_cast<float2 *>(w + 256);
+            MFEM_CUDA(cudaMemsetAsync(xsp.xmax, 0, sizeof(unsigned long long), s));
+            k_xmax<<<(unsigned)std::min<long long>(blocks_for(n, kThreads), kMaxCtas), kThreads, 0, s>>>(x, n, xsp.xmax);
+            check_launch("k_xmax");
+        }
+        k_split_x<D><<<blocks_for(n, kThreads), kThreads, 0, s>>>(x, xsp.xs, n, xsp.xmax, mask, stop);
+        check_launch("k_split_x");
+        const long long nv = (long long)c.nnz * D * D;
+        if (partial)
+            k_spmv32<D, true><<<grid32, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<float>(),
+                                                        nv, xsp.xs, xsp.xmax, x, y, c.nbNodes, mask, partial, stop);
+        else
+            k_spmv32<D, false><<<grid32, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<float>(),
+                                                         nv, xsp.xs, xsp.xmax, x, y, c.nbNodes, mask, nullptr, stop);
+    } else {
         k_spmv<double, D><<<grid, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<double>(),
                                                     x, y, c.nbNodes, mask, partial, stop);
+    }
     check_launch("k_spmv");
 }
 
-void spmv(const Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
-          const int *stop = nullptr) {
-    if (op_dim_of(c) == 9) spmv_t<3>(c, x, y, mask, partial, stop, c.stream);
-    else spmv_t<1>(c, x, y, mask, partial, stop, c.stream);
+void spmv(Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
+          const int *stop = nullptr, XSplit xsp = {}) {
+    if (op_dim_of(c) == 9) spmv_t<3>(c, x, y, mask, partial, stop, xsp, c.stream);
+    else spmv_t<1>(c, x, y, mask, partial, stop, xsp, c.stream);
 }
 
 // CG iterations enqueued between two looks at the convergence flag
@@ -314,12 +610,18 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     MFEM_REQUIRE(maxIter >= 0, MFEM_ERR_INVALID_ARG, "negative maxIter");
     const int D = op_dim_of(c) == 9 ? 3 : 1;
     const size_t n = (size_t)c.nbNodes * D;
-    const int nCtaRows = (int)blocks_for(c.nbNodes, kRowsPerCta);
+    const int nCtaRows = (int)blocks_for(c.nbNodes, c.lastPrecision == MFEM_FP32 ? kRows32 : kRowsPerCta);
     const int nCtaNodes = (int)blocks_for(c.nbNodes, kThreads);
     const int nCta = std::max(nCtaRows, nCtaNodes);
-    double *w = (double *)c.solver.reserve(sizeof(double) * (6 * n + 3 * (size_t)nCta + 8) + sizeof(CgScalars) + 64);
+    double *w = (double *)c.solver.reserve(sizeof(double) * (7 * n + 3 * (size_t)nCta + 9) + sizeof(CgScalars) + 64);
     double *vb = w, *vx = w + n, *vr = w + 2 * n, *vz = w + 3 * n, *vp = w + 4 * n, *vq = w + 5 * n;
-    double *partial = w + 6 * n;
+    // hi/lo split of p and max |p| for the FP32-valued operator (none for FP64 values)
+    XSplit ps;
+    if (c.lastPrecision == MFEM_FP32) {
+        ps.xs = reinterpret_cast<float2 *>(w + 6 * n);
+        ps.xmax = reinterpret_cast<unsigned long long *>(w + 7 * n);
+    }
+    double *partial = w + 7 * n + 1;
     double *sums = partial + 3 * (size_t)nCta;
     CgScalars *sc = reinterpret_cast<CgScalars *>(sums + 8);
     CgScalars *hostSc = nullptr;
@@ -335,8 +637,9 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     const double *P = c.prec.as<double>();
     // r = b - A x, z = P r, p = z
     spmv(c, vx, vq, mask, nullptr);
-    if (D == 3) k_cg_init<3><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, c.nbNodes, partial, nCtaNodes);
-    else k_cg_init<1><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, c.nbNodes, partial, nCtaNodes);
+    if (ps.xmax) MFEM_CUDA(cudaMemsetAsync(ps.xmax, 0, sizeof(unsigned long long), s));
+    if (D == 3) k_cg_init<3><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, ps.xmax, c.nbNodes, partial, nCtaNodes);
+    else k_cg_init<1><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, ps.xmax, c.nbNodes, partial, nCtaNodes);
     check_launch("k_cg_init");
     k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 3, sums, nullptr);
     k_cg_start<<<1, 1, 0, s>>>(sc, sums, rtol * rtol, maxIter);
@@ -347,14 +650,15 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     const int *stop = &sc->stop;
     while (!hostSc->stop) {
         for (int k = 0; k < kCgBatch; k++) {
-            spmv(c, vp, vq, mask, partial, stop);              // q = A p, partials of p . q
+            spmv(c, vp, vq, mask, partial, stop, ps);          // q = A p, partials of p . q
             k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaRows, 1, sums, stop);
             k_cg_alpha<<<1, 1, 0, s>>>(sc, sums);
             if (D == 3) k_cg_update<3><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
             else k_cg_update<1><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
             k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 2, sums, stop);
-            k_cg_beta<<<1, 1, 0, s>>>(sc, sums);
-            k_cg_direction<<<blocks_for((long long)n, kThreads), kThreads, 0, s>>>(sc, vz, vp, (long long)n);
+            k_cg_beta<<<1, 1, 0, s>>>(sc, sums, ps.xmax);
+            k_cg_direction<<<(unsigned)std::min<long long>(blocks_for((long long)n, kThreads), kMaxCtas), kThreads, 0, s>>>(
+                sc, vz, vp, ps.xmax, (long long)n);
         }
         check_launch("k_cg iteration");
         MFEM_CUDA(cudaMemcpyAsync(hostSc, sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));

@@ -106,6 +106,32 @@ __device__ __forceinline__ void ela_accumulate(Kahan *acc, float4 gj, float4 gk,
     }
 }
 
+// Two elasticity contributions (j0, k0), (j1, k1) added to the block as one
+// term per entry: the pair's sum is formed by an FMA on the first
+// contribution's value (one rounding at the pair's magnitude where the single
+// form rounds each product), then added with compensation, so that the pair
+// costs one compensated addition per entry instead of two.
+__device__ __forceinline__ void ela_accumulate2(Kahan *acc, float4 gj0, float4 gk0, float2 w0,
+                                                float4 gj1, float4 gk1, float2 w1, bool first) {
+    const float bx0 = gk0.x * w0.x, by0 = gk0.y * w0.x, bz0 = gk0.z * w0.x;
+    const float bx1 = gk1.x * w1.x, by1 = gk1.y * w1.x, bz1 = gk1.z * w1.x;
+    const float md0 = w0.y * fmaf(gj0.x, gk0.x, fmaf(gj0.y, gk0.y, gj0.z * gk0.z));
+    const float md = fmaf(w1.y, fmaf(gj1.x, gk1.x, fmaf(gj1.y, gk1.y, gj1.z * gk1.z)), md0);
+    const float c[9] = {fmaf(gj1.x, bx1, fmaf(gj0.x, bx0, md)), fmaf(gj1.x, by1, gj0.x * by0),
+                        fmaf(gj1.x, bz1, gj0.x * bz0),
+                        fmaf(gj1.y, bx1, gj0.y * bx0), fmaf(gj1.y, by1, fmaf(gj0.y, by0, md)),
+                        fmaf(gj1.y, bz1, gj0.y * bz0),
+                        fmaf(gj1.z, bx1, gj0.z * bx0), fmaf(gj1.z, by1, gj0.z * by0),
+                        fmaf(gj1.z, bz1, fmaf(gj0.z, bz0, md))};
+    if (first) {
+#pragma unroll
+        for (int m = 0; m < 9; m++) { acc[m].s = c[m]; acc[m].c = 0.f; }
+    } else {
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc[m].add(c[m]);
+    }
+}
+
 // One 3x3 FP32 block to base[9p .. 9p+8] with three or four 16-, 8- and
 // 4-byte stores chosen by the block's address modulo 16, instead of nine 4-byte
 // stores: fewer memory transactions per block.
@@ -164,15 +190,20 @@ __device__ __forceinline__ void ela_diag_accumulate(Kahan *acc, float4 g, float 
     acc[5].add(g.y * bz);
 }
 
-// x * 2^k, exact, by exponent arithmetic on the integer pipe when x and the
-// result are normal; otherwise (zero, subnormal, out of range) by a multiply.
-__device__ __forceinline__ double scale_pow2(double x, int k) {
-    const long long b = __double_as_longlong(x);
-    const int e = (int)((b >> 52) & 0x7ff);
-    if (e > 0 && e + k > 0 && e + k < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
-    if (x == 0.0) return x;
-    const int kk = max(-1022, min(1023, k));
-    return x * __longlong_as_double((long long)(kk + 1023) << 52);
+// Two contributions to a diagonal block as one term per entry (as
+// ela_accumulate2).
+__device__ __forceinline__ void ela_diag_accumulate2(Kahan *acc, float4 g0, float2 w0, float4 g1,
+                                                     float2 w1) {
+    const float bx0 = g0.x * w0.x, by0 = g0.y * w0.x, bz0 = g0.z * w0.x;
+    const float bx1 = g1.x * w1.x, by1 = g1.y * w1.x, bz1 = g1.z * w1.x;
+    const float md0 = w0.y * fmaf(g0.x, g0.x, fmaf(g0.y, g0.y, g0.z * g0.z));
+    const float md = fmaf(w1.y, fmaf(g1.x, g1.x, fmaf(g1.y, g1.y, g1.z * g1.z)), md0);
+    acc[0].add(fmaf(g1.x, bx1, fmaf(g0.x, bx0, md)));
+    acc[1].add(fmaf(g1.y, by1, fmaf(g0.y, by0, md)));
+    acc[2].add(fmaf(g1.z, bz1, fmaf(g0.z, bz0, md)));
+    acc[3].add(fmaf(g1.x, by1, g0.x * by0));
+    acc[4].add(fmaf(g1.x, bz1, g0.x * bz0));
+    acc[5].add(fmaf(g1.y, bz1, g0.y * bz0));
 }
 
 // 1 / x in FP64: the FP32 reciprocal of x (relative error below 2^-23) refined by
@@ -391,10 +422,15 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 }
             } else {
                 Kahan acc[6];
-                for (int q = b + part; q < b + n; q += 4) {
+                // this lane's contributions two at a time, each pair one term
+                int q = b + part;
+                for (; q + 4 < b + n; q += 8) {
+                    const unsigned u0 = sC[q], u1 = sC[q + 4];
+                    ela_diag_accumulate2(acc, G[slot_j(u0)], W[u0 >> 4], G[slot_j(u1)], W[u1 >> 4]);
+                }
+                if (q < b + n) {
                     const unsigned u = sC[q];
-                    const int l = u >> 4;
-                    const float2 w = W[l];
+                    const float2 w = W[u >> 4];
                     ela_diag_accumulate(acc, G[slot_j(u)], w.x, w.y);
                 }
 #pragma unroll
@@ -482,16 +518,15 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 if (ent.y >= 0) values[ent.y] = v;
             } else {
                 Kahan acc[9];
-                // two contributions per pass: their shared-memory loads are in
-                // flight together (same summation order as one at a time)
+                // two contributions per pass, summed as one term (their
+                // shared-memory loads are in flight together)
                 int q = b;
                 for (; q + 1 < b + n; q += 2) {
                     const unsigned u0 = sC[q], u1 = sC[q + 1];
                     const float4 gj0 = G[slot_j(u0)], gk0 = G[slot_k(u0)];
                     const float4 gj1 = G[slot_j(u1)], gk1 = G[slot_k(u1)];
                     const float2 w0 = W[u0 >> 4], w1 = W[u1 >> 4];
-                    ela_accumulate(acc, gj0, gk0, w0.x, w0.y, q == b);
-                    ela_accumulate(acc, gj1, gk1, w1.x, w1.y, false);
+                    ela_accumulate2(acc, gj0, gk0, w0, gj1, gk1, w1, q == b);
                 }
                 if (q < b + n) {
                     const unsigned u = sC[q];

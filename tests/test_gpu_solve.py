@@ -45,7 +45,7 @@ def _dev(x):
     return torch.from_numpy(np.ascontiguousarray(x)).cuda()
 
 
-@pytest.mark.parametrize("op,precision", [("ela", "fp64"), ("ela", "fp32"), ("lap", "fp64")])
+@pytest.mark.parametrize("op,precision", [("ela", "fp64"), ("ela", "fp32"), ("lap", "fp64"), ("lap", "fp32")])
 @pytest.mark.parametrize("constrained", [False, True])
 def test_spmv_matches_scipy(gpu, op, precision, constrained):
     m, a, row, col, vals, prec, markf = _assembled(gpu, op, precision=precision)
@@ -67,6 +67,69 @@ def test_spmv_matches_scipy(gpu, op, precision, constrained):
     # summation order differs from scipy's: relative to the row's magnitude sum
     scale = abs(A) @ abs(x) + abs(x)
     assert np.max(np.abs(y - ref) / scale) < 1e-13
+
+
+def _spmv(a, x):
+    xd = _dev(x)
+    yd = torch.empty(len(x), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    a.spmv(xd.data_ptr(), yd.data_ptr(), False)
+    a.synchronize()
+    torch.cuda.synchronize()
+    return yd.cpu().numpy()
+
+
+@pytest.mark.parametrize("op", ["ela", "lap"])
+def test_spmv_fp32_values_any_scale(gpu, op):
+    """FP32 values: x is scaled by a power of two and split into FP32 parts;
+    rows the split cannot serve (entries far below the largest, all-zero rows)
+    take the FP64 chain.  Every case within 1e-13 of the row's magnitude sum,
+    exact zeros where every product is zero."""
+    m, a, row, col, vals, prec, markf = _assembled(gpu, op, precision="fp32")
+    dim = 1 if op == "lap" else 3
+    N = len(row) - 1
+    A = _matrix(row, col, vals, dim)
+    n = N * dim
+    rng = np.random.default_rng(7)
+    cases = {
+        "tiny": rng.standard_normal(n) * 1e-200,
+        "huge": rng.standard_normal(n) * 1e200,
+        "spread": rng.standard_normal(n) * 10.0 ** rng.uniform(-40, 40, n),
+        "sparse": np.where(rng.random(n) < 0.05, rng.standard_normal(n), 0.0),
+        "zero": np.zeros(n),
+    }
+    for name, x in cases.items():
+        y = _spmv(a, x)
+        ref = A @ x
+        scale = abs(A) @ abs(x)
+        live = scale > 0
+        assert np.all(y[~live] == 0.0), name
+        assert np.max(np.abs(y[live] - ref[live]) / scale[live], initial=0.0) < 1e-13, name
+
+
+def test_spmv_fp32_values_non_finite(gpu):
+    """A NaN or infinite x entry: the rows whose pattern holds its node come out
+    NaN or infinite as with FP64 values; every other row is unaffected."""
+    m, a, row, col, vals, prec, markf = _assembled(gpu, "ela", precision="fp32")
+    N = len(row) - 1
+    A = _matrix(row, col, vals, 3)
+    rng = np.random.default_rng(8)
+    for bad in (np.nan, np.inf):
+        x = rng.standard_normal(3 * N)
+        node = N // 2
+        x[3 * node + 1] = bad
+        y = _spmv(a, x)
+        rows = np.repeat(np.arange(N), np.diff(row))
+        hit = np.zeros(N, bool)
+        hit[rows[col - 1 == node]] = True
+        hit3 = np.repeat(hit, 3)
+        assert not np.isfinite(y[hit3]).any()
+        xf = np.where(np.isfinite(x), x, 0.0)
+        ref = A @ xf
+        scale = abs(A) @ abs(xf)
+        ok = ~hit3
+        assert np.isfinite(y[ok]).all()
+        assert np.max(np.abs(y[ok] - ref[ok]) / scale[ok]) < 1e-13
 
 
 def test_prec_apply_matches_blocks(gpu):
