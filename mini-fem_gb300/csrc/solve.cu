@@ -47,6 +47,78 @@ __device__ __forceinline__ void cta_sum(double v, double *partial) {
     }
 }
 
+// Scalars of the CG recurrence, kept on the device.
+struct CgScalars {
+    double rz, pq, alpha, beta, rr, bb, tol2;
+    int iter, maxIter, stop;   // stop: converged or out of iterations; later kernels do nothing
+};
+
+// What a CG kernel needs to finish its own reduction: the CTA that completes
+// last sums the CTA partials and updates the scalars, so that no separate
+// reduction launch follows.  sc == nullptr: not inside CG.
+struct CgLink {
+    CgScalars *sc = nullptr;
+    double *sums = nullptr;
+    unsigned *counter = nullptr;              // CTAs done; zero between kernels
+    unsigned long long *scaleMax = nullptr;   // FP32 values: max |p| the split of p used
+    unsigned long long *nextMax = nullptr;    //   and max |p| of the p being formed
+};
+
+// Sums of nSums arrays of nCta partials, each in index order by a strided sum
+// per thread and a fixed tree: run by the CTA that finishes last, which then
+// calls `then` on one thread.  Every thread of the grid calls it after its
+// CTA's partials are written; the counter is left at zero.  t: kThreads
+// doubles of shared memory the caller no longer needs (its staging buffer),
+// so that the kernel's shared-memory footprint does not grow.
+template <class F>
+__device__ __forceinline__ void last_cta_sums(const double *partial, int nCta, int nSums, double *sums,
+                                              unsigned *counter, double *t, F then) {
+    __shared__ bool last;
+    __threadfence();   // the partials written by this CTA, before its count
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int k = 0; k < nSums; k++) {
+        double v = 0.0;
+        for (int i = threadIdx.x; i < nCta; i += kThreads) v += __ldcg(partial + (size_t)k * nCta + i);
+        t[threadIdx.x] = v;
+        __syncthreads();
+        for (int w = kThreads / 2; w >= 1; w >>= 1) {
+            if ((int)threadIdx.x < w) t[threadIdx.x] += t[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) sums[k] = t[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        then(sums);
+        *counter = 0u;
+    }
+}
+
+// alpha = (r . z) / (p . q)
+__device__ __forceinline__ void cg_alpha(CgScalars *sc, const double *sums) {
+    sc->pq = sums[0];
+    sc->alpha = sc->pq != 0.0 ? sc->rz / sc->pq : 0.0;
+}
+
+// beta, the new r . z and r . r, the stop test; for FP32 values the max of the
+// current p becomes the scale of the next p's split
+__device__ __forceinline__ void cg_beta(CgScalars *sc, const double *sums, CgLink link) {
+    const double rzNew = sums[0];
+    sc->beta = sc->rz != 0.0 ? rzNew / sc->rz : 0.0;
+    sc->rz = rzNew;
+    sc->rr = sums[1];
+    sc->iter++;
+    if (sc->rr <= sc->tol2 * sc->bb || sc->iter >= sc->maxIter) sc->stop = 1;
+    if (link.scaleMax) {
+        *link.scaleMax = *link.nextMax;
+        *link.nextMax = 0ull;
+    }
+}
+
 __device__ __forceinline__ bool constrained(const unsigned char *mask, int node, int k, int dim) {
     return mask && (dim == 1 ? mask[node] != 0 : ((mask[node] >> k) & 1u));
 }
@@ -60,7 +132,7 @@ __global__ void __launch_bounds__(kThreads)
 k_spmv(const int *__restrict__ rowPtr, const int *__restrict__ col, const V *__restrict__ vals,
        const double *__restrict__ x, double *__restrict__ y, int N,
        const unsigned char *__restrict__ mask, double *__restrict__ partial,
-       const int *__restrict__ stop) {
+       const int *__restrict__ stop, CgLink link) {
     if (stop && *stop) return;   // CG: converged in an earlier iteration of the batch
     constexpr int B = D * D;
     __shared__ V sv[kRowsPerCta][kLanesPerRow * B];
@@ -111,6 +183,10 @@ k_spmv(const int *__restrict__ rowPtr, const int *__restrict__ col, const V *__r
         }
     }
     if (partial) cta_sum(dot, partial);
+    static_assert(sizeof(sv) >= sizeof(double) * kThreads, "staging buffer reused by the reduction");
+    if (link.sc)
+        last_cta_sums(partial, (int)gridDim.x, 1, link.sums, link.counter, reinterpret_cast<double *>(&sv[0][0]),
+                      [&](const double *sm) { cg_alpha(link.sc, sm); });
 }
 
 // ---- FP32 values: the operator without the FP64 pipe ----
@@ -228,9 +304,10 @@ k_spmv32(const int *__restrict__ rowPtr, const int *__restrict__ col, const floa
          long long nVals, const float2 *__restrict__ xs, const unsigned long long *__restrict__ xmax,
          const double *__restrict__ x, double *__restrict__ y, int N,
          const unsigned char *__restrict__ mask, double *__restrict__ partial,
-         const int *__restrict__ stop) {
+         const int *__restrict__ stop, CgLink link) {
     if (stop && *stop) return;
     constexpr int B = D * D, BPL = kSpmvBlocksPerLane, CH = kLanes32 * BPL;
+    static_assert(kLanes32 >= D, "one lane per output component");
     // a chunk's values from the 16-byte boundary at or below its start: at
     // most 3 leading floats, whole 16-byte pieces
     constexpr int kPieces = (3 + CH * B + 3) / 4, kRow = 4 * kPieces;
@@ -351,20 +428,26 @@ k_spmv32(const int *__restrict__ rowPtr, const int *__restrict__ col, const floa
 #pragma unroll
             for (int d = 0; d < D; d++) a[d] += __shfl_xor_sync(0xffffffffu, a[d], off);
     }
+    // every lane holds the row's sums: lane d writes component d (one FP64
+    // addition per lane instead of D on one lane)
     double dot = 0.0;
-    if (row < N && sub == 0) {
-        const int kx = scale_exp(xmax);
+    if (row < N && sub < D) {
+        float sd = s[0], td = t[0];
+        double ad = a[0];
 #pragma unroll
-        for (int d = 0; d < D; d++) {
-            const double xv = x[(size_t)row * D + d];
-            double yv = a[d];
-            if (!bad) yv = scale_pow2(f32_to_f64(s[d]) + f32_to_f64(t[d]), kx);
-            if (constrained(mask, row, d, D)) yv = xv;
-            y[(size_t)row * D + d] = yv;
-            if (DOT) dot = fma(xv, yv, dot);
-        }
+        for (int d = 1; d < D; d++)
+            if (sub == d) { sd = s[d]; td = t[d]; ad = a[d]; }
+        const double xv = x[(size_t)row * D + sub];
+        double yv = bad ? ad : scale_pow2(f32_to_f64(sd) + f32_to_f64(td), scale_exp(xmax));
+        if (constrained(mask, row, sub, D)) yv = xv;
+        y[(size_t)row * D + sub] = yv;
+        if (DOT) dot = xv * yv;
     }
     if (DOT) cta_sum(dot, partial);
+    static_assert(sizeof(sv) >= sizeof(double) * kThreads, "staging buffer reused by the reduction");
+    if (DOT && link.sc)
+        last_cta_sums(partial, (int)gridDim.x, 1, link.sums, link.counter, reinterpret_cast<double *>(&sv[0][0]),
+                      [&](const double *sm) { cg_alpha(link.sc, sm); });
 }
 
 // z = P r (block-Jacobi), one thread per node.
@@ -382,12 +465,6 @@ __global__ void k_prec_apply(const double *__restrict__ prec, const double *__re
         z[(size_t)i * D + a] = s;
     }
 }
-
-// Scalars of the CG recurrence, kept on the device.
-struct CgScalars {
-    double rz, pq, alpha, beta, rr, bb, tol2;
-    int iter, maxIter, stop;   // stop: converged or out of iterations; later kernels do nothing
-};
 
 // r = b - A x (A x already in q); z = P r; partials of r . z, r . r and b . b.
 template <int D>
@@ -448,7 +525,8 @@ __global__ void k_sum_partials(const double *__restrict__ partial, int nCta, int
     }
 }
 
-__global__ void k_cg_start(CgScalars *sc, const double *sums, double tol2, int maxIter) {
+__global__ void k_cg_start(CgScalars *sc, const double *sums, double tol2, int maxIter, CgLink link) {
+    if (link.scaleMax) *link.scaleMax = *link.nextMax;   // the scale of p's first split
     sc->rz = sums[0];
     sc->rr = sums[1];
     sc->bb = sums[2];
@@ -458,19 +536,13 @@ __global__ void k_cg_start(CgScalars *sc, const double *sums, double tol2, int m
     sc->stop = (sc->rr <= tol2 * sc->bb || maxIter <= 0) ? 1 : 0;
 }
 
-__global__ void k_cg_alpha(CgScalars *sc, const double *sums) {
-    if (sc->stop) return;
-    sc->pq = sums[0];
-    sc->alpha = sc->pq != 0.0 ? sc->rz / sc->pq : 0.0;
-}
-
 // x += alpha p; r -= alpha q; z = P r; partials of r . z and r . r.
 template <int D>
 __global__ void __launch_bounds__(kThreads)
-k_cg_update(const double *__restrict__ prec, const CgScalars *__restrict__ sc,
+k_cg_update(const double *__restrict__ prec, CgScalars *__restrict__ sc,
             const double *__restrict__ p, const double *__restrict__ q, double *__restrict__ x,
             double *__restrict__ r, double *__restrict__ z, int N, double *__restrict__ partial,
-            int nCta) {
+            int nCta, CgLink link) {
     if (sc->stop) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double alpha = sc->alpha;
@@ -498,34 +570,35 @@ k_cg_update(const double *__restrict__ prec, const CgScalars *__restrict__ sc,
     cta_sum(rz, partial);
     __syncthreads();
     cta_sum(rr, partial + nCta);
+    __shared__ double t[kThreads];
+    last_cta_sums(partial, nCta, 2, link.sums, link.counter, t,
+                  [&](const double *sm) { cg_beta(sc, sm, link); });
 }
 
-__global__ void k_cg_beta(CgScalars *sc, const double *sums, unsigned long long *pmax) {
-    if (sc->stop) return;
-    if (pmax) *pmax = 0;
-    const double rzNew = sums[0];
-    sc->beta = sc->rz != 0.0 ? rzNew / sc->rz : 0.0;
-    sc->rz = rzNew;
-    sc->rr = sums[1];
-    sc->iter++;
-    if (sc->rr <= sc->tol2 * sc->bb || sc->iter >= sc->maxIter) sc->stop = 1;
-}
-
-// p = z + beta p (and, for the FP32-valued operator, max |p| into *pmax,
-// which k_cg_beta cleared); grid-stride
+// p = z + beta p; grid-stride.  For the FP32-valued operator also the split
+// of p (constrained DOFs zero) at the scale of *link.scaleMax, the previous
+// p's maximum, which the operator then uses, and max |p| into *link.nextMax
+// for the next split.  A scale from the previous p only shifts where the split
+// range lies: entries it cannot serve are marked and their rows take FP64.
+template <int D>
 __global__ void __launch_bounds__(kThreads)
-k_cg_direction(const CgScalars *__restrict__ sc, const double *__restrict__ z,
-               double *__restrict__ p, unsigned long long *__restrict__ pmax, long long n) {
+k_cg_direction(const CgScalars *__restrict__ sc, const double *__restrict__ z, double *__restrict__ p,
+               float2 *__restrict__ ps, const unsigned char *__restrict__ mask, long long n, CgLink link) {
     if (sc->stop) return;
     const double beta = sc->beta;
+    const int kx = ps ? scale_exp(link.scaleMax) : 0;
     unsigned long long pm = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double v = fma(beta, p[i], z[i]);
         p[i] = v;
-        const unsigned long long b = abs_bits(v);
-        pm = b > pm ? b : pm;
+        if (ps) {
+            const bool c = mask && constrained(mask, (int)(i / D), (int)(i % D), D);
+            ps[i] = c ? make_float2(0.f, 0.f) : split_x(v, kx);
+            const unsigned long long b = abs_bits(v);
+            pm = b > pm ? b : pm;
+        }
     }
-    if (pmax) block_max_into(pm, pmax);
+    if (ps) block_max_into(pm, link.nextMax);
 }
 
 // Split of an SpMV operand for FP32 values: its hi/lo parts and the largest
@@ -533,45 +606,50 @@ k_cg_direction(const CgScalars *__restrict__ sc, const double *__restrict__ z,
 struct XSplit {
     float2 *xs = nullptr;
     unsigned long long *xmax = nullptr;
+    bool ready = false;   // xs already holds the split at the scale of *xmax (CG)
 };
 
-// FP32 values: the split of x made here (into c.xsplit) unless given with its
-// maximum already in xsp.xmax (the CG direction).
+// FP32 values: the split of x made here (into c.xsplit) unless given ready.
+// Inside CG (link.sc set) the operator also finishes p . q and alpha.
 template <int D>
 void spmv_t(Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
-            const int *stop, XSplit xsp, cudaStream_t s) {
+            const int *stop, XSplit xsp, CgLink link, cudaStream_t s) {
     const unsigned grid = blocks_for(c.nbNodes, kRowsPerCta);
     if (c.lastPrecision == MFEM_FP32) {
         const unsigned grid32 = blocks_for(c.nbNodes, kRows32);
         const long long n = (long long)c.nbNodes * D;
-        if (!xsp.xs) {
-            char *w = (char *)c.xsplit.reserve(sizeof(float2) * (size_t)n + 256);
-            xsp.xmax = reinterpret_cast<unsigned long long *>(w);
-            xsp.xs = reinterpret_cast<float2 *>(w + 256);
+        if (!xsp.ready) {
+            if (!xsp.xs) {
+                char *w = (char *)c.xsplit.reserve(sizeof(float2) * (size_t)n + 256);
+                xsp.xmax = reinterpret_cast<unsigned long long *>(w);
+                xsp.xs = reinterpret_cast<float2 *>(w + 256);
+            }
             MFEM_CUDA(cudaMemsetAsync(xsp.xmax, 0, sizeof(unsigned long long), s));
             k_xmax<<<(unsigned)std::min<long long>(blocks_for(n, kThreads), kMaxCtas), kThreads, 0, s>>>(x, n, xsp.xmax);
             check_launch("k_xmax");
+            k_split_x<D><<<blocks_for(n, kThreads), kThreads, 0, s>>>(x, xsp.xs, n, xsp.xmax, mask, stop);
+            check_launch("k_split_x");
         }
-        k_split_x<D><<<blocks_for(n, kThreads), kThreads, 0, s>>>(x, xsp.xs, n, xsp.xmax, mask, stop);
-        check_launch("k_split_x");
         const long long nv = (long long)c.nnz * D * D;
         if (partial)
             k_spmv32<D, true><<<grid32, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<float>(),
-                                                        nv, xsp.xs, xsp.xmax, x, y, c.nbNodes, mask, partial, stop);
+                                                        nv, xsp.xs, xsp.xmax, x, y, c.nbNodes, mask, partial, stop,
+                                                        link);
         else
             k_spmv32<D, false><<<grid32, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<float>(),
-                                                         nv, xsp.xs, xsp.xmax, x, y, c.nbNodes, mask, nullptr, stop);
+                                                         nv, xsp.xs, xsp.xmax, x, y, c.nbNodes, mask, nullptr, stop,
+                                                         CgLink{});
     } else {
         k_spmv<double, D><<<grid, kThreads, 0, s>>>(c.rowPtr.as<int>(), c.col.as<int>(), c.values.as<double>(),
-                                                    x, y, c.nbNodes, mask, partial, stop);
+                                                    x, y, c.nbNodes, mask, partial, stop, link);
     }
     check_launch("k_spmv");
 }
 
 void spmv(Context &c, const double *x, double *y, const unsigned char *mask, double *partial,
-          const int *stop = nullptr, XSplit xsp = {}) {
-    if (op_dim_of(c) == 9) spmv_t<3>(c, x, y, mask, partial, stop, xsp, c.stream);
-    else spmv_t<1>(c, x, y, mask, partial, stop, xsp, c.stream);
+          const int *stop = nullptr, XSplit xsp = {}, CgLink link = {}) {
+    if (op_dim_of(c) == 9) spmv_t<3>(c, x, y, mask, partial, stop, xsp, link, c.stream);
+    else spmv_t<1>(c, x, y, mask, partial, stop, xsp, link, c.stream);
 }
 
 // CG iterations enqueued between two looks at the convergence flag
@@ -613,17 +691,25 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     const int nCtaRows = (int)blocks_for(c.nbNodes, c.lastPrecision == MFEM_FP32 ? kRows32 : kRowsPerCta);
     const int nCtaNodes = (int)blocks_for(c.nbNodes, kThreads);
     const int nCta = std::max(nCtaRows, nCtaNodes);
-    double *w = (double *)c.solver.reserve(sizeof(double) * (7 * n + 3 * (size_t)nCta + 9) + sizeof(CgScalars) + 64);
+    double *w = (double *)c.solver.reserve(sizeof(double) * (7 * n + 3 * (size_t)nCta + 12) + sizeof(CgScalars) + 64);
     double *vb = w, *vx = w + n, *vr = w + 2 * n, *vz = w + 3 * n, *vp = w + 4 * n, *vq = w + 5 * n;
-    // hi/lo split of p and max |p| for the FP32-valued operator (none for FP64 values)
+    double *partial = w + 7 * n + 3;
+    double *sums = partial + 3 * (size_t)nCta;
+    CgScalars *sc = reinterpret_cast<CgScalars *>(sums + 8);
+    // the fused reductions' CTA counter; for FP32 values the split of p (made
+    // by the direction update) and the two maxima of |p|
+    CgLink link;
+    link.sc = sc;
+    link.sums = sums;
+    link.counter = reinterpret_cast<unsigned *>(w + 7 * n);
     XSplit ps;
     if (c.lastPrecision == MFEM_FP32) {
         ps.xs = reinterpret_cast<float2 *>(w + 6 * n);
-        ps.xmax = reinterpret_cast<unsigned long long *>(w + 7 * n);
+        link.scaleMax = reinterpret_cast<unsigned long long *>(w + 7 * n + 1);
+        link.nextMax = reinterpret_cast<unsigned long long *>(w + 7 * n + 2);
+        ps.xmax = link.scaleMax;
+        ps.ready = true;
     }
-    double *partial = w + 7 * n + 1;
-    double *sums = partial + 3 * (size_t)nCta;
-    CgScalars *sc = reinterpret_cast<CgScalars *>(sums + 8);
     CgScalars *hostSc = nullptr;
     MFEM_CUDA(cudaMallocHost(&hostSc, sizeof(CgScalars)));
     struct Free {
@@ -634,31 +720,35 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     cudaStream_t s = c.stream;
     MFEM_CUDA(cudaMemcpyAsync(vb, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     MFEM_CUDA(cudaMemcpyAsync(vx, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    MFEM_CUDA(cudaMemsetAsync(w + 7 * n, 0, 3 * sizeof(double), s));   // counter, maxima
     const double *P = c.prec.as<double>();
-    // r = b - A x, z = P r, p = z
+    // r = b - A x, z = P r, p = z (and max |p|), then the split of p at that
+    // maximum, which becomes the scale the first iterations use
     spmv(c, vx, vq, mask, nullptr);
-    if (ps.xmax) MFEM_CUDA(cudaMemsetAsync(ps.xmax, 0, sizeof(unsigned long long), s));
-    if (D == 3) k_cg_init<3><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, ps.xmax, c.nbNodes, partial, nCtaNodes);
-    else k_cg_init<1><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, ps.xmax, c.nbNodes, partial, nCtaNodes);
+    if (D == 3) k_cg_init<3><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, link.nextMax, c.nbNodes, partial, nCtaNodes);
+    else k_cg_init<1><<<nCtaNodes, kThreads, 0, s>>>(P, vb, vq, vr, vz, vp, link.nextMax, c.nbNodes, partial, nCtaNodes);
     check_launch("k_cg_init");
+    if (ps.xs) {
+        if (D == 3) k_split_x<3><<<blocks_for((long long)n, kThreads), kThreads, 0, s>>>(vp, ps.xs, (long long)n, link.nextMax, mask, nullptr);
+        else k_split_x<1><<<blocks_for((long long)n, kThreads), kThreads, 0, s>>>(vp, ps.xs, (long long)n, link.nextMax, mask, nullptr);
+        check_launch("k_split_x");
+    }
     k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 3, sums, nullptr);
-    k_cg_start<<<1, 1, 0, s>>>(sc, sums, rtol * rtol, maxIter);
+    k_cg_start<<<1, 1, 0, s>>>(sc, sums, rtol * rtol, maxIter, link);
     MFEM_CUDA(cudaMemcpyAsync(hostSc, sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));
     MFEM_CUDA(cudaStreamSynchronize(s));
-    // batches of iterations; every kernel of an iteration after the one that
-    // met the tolerance returns at once, so the iterate stays the converged one
+    // batches of iterations, three launches each (operator + alpha, update +
+    // beta, direction); every kernel of an iteration after the one that met
+    // the tolerance returns at once, so the iterate stays the converged one
     const int *stop = &sc->stop;
+    const unsigned gDir = (unsigned)std::min<long long>(blocks_for((long long)n, kThreads), kMaxCtas);
     while (!hostSc->stop) {
         for (int k = 0; k < kCgBatch; k++) {
-            spmv(c, vp, vq, mask, partial, stop, ps);          // q = A p, partials of p . q
-            k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaRows, 1, sums, stop);
-            k_cg_alpha<<<1, 1, 0, s>>>(sc, sums);
-            if (D == 3) k_cg_update<3><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
-            else k_cg_update<1><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes);
-            k_sum_partials<<<1, kThreads, 0, s>>>(partial, nCtaNodes, 2, sums, stop);
-            k_cg_beta<<<1, 1, 0, s>>>(sc, sums, ps.xmax);
-            k_cg_direction<<<(unsigned)std::min<long long>(blocks_for((long long)n, kThreads), kMaxCtas), kThreads, 0, s>>>(
-                sc, vz, vp, ps.xmax, (long long)n);
+            spmv(c, vp, vq, mask, partial, stop, ps, link);     // q = A p; p . q; alpha
+            if (D == 3) k_cg_update<3><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes, link);
+            else k_cg_update<1><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes, link);
+            if (D == 3) k_cg_direction<3><<<gDir, kThreads, 0, s>>>(sc, vz, vp, ps.xs, mask, (long long)n, link);
+            else k_cg_direction<1><<<gDir, kThreads, 0, s>>>(sc, vz, vp, ps.xs, mask, (long long)n, link);
         }
         check_launch("k_cg iteration");
         MFEM_CUDA(cudaMemcpyAsync(hostSc, sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, s));

@@ -25,7 +25,9 @@
 //   3b. one thread per row (the first warps) masks the block and inverts it in
 //      FP64 into the preconditioner, while the other warps run phase 2;
 //   2. one thread per off-diagonal entry sums its contributions with Kahan
-//      compensation and writes the 3x3 block (or scalar) to the CSR values;
+//      compensation (ela: two contributions per compensated addition, their
+//      sum formed by an FMA) and writes the 3x3 block (or scalar) to the CSR
+//      values;
 //      warps take 32 entries at a time from a shared counter, so that the warps
 //      of 3a and 3b join when their work is done.
 // The plan is built once per mesh and pattern on the device (tileplan.cu).
