@@ -168,6 +168,22 @@ def test_pcg_solves_constrained_system(gpu, op, precision):
     assert it2 == it and x2.tobytes() == x.tobytes()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pcg_scale_equivariant(gpu, precision):
+    """b times a power of two gives the same iterations and exactly the solution
+    times that power: every reduction, alpha and beta is scale-free in FP64,
+    and the FP32-valued operator's split follows the scale of p (the FP32
+    arithmetic then sees the same significands), over 600 binary orders."""
+    m, a, row, col, vals, prec, markf = _assembled(gpu, "ela", n=9, precision=precision)
+    N = len(row) - 1
+    b = np.random.default_rng(11).standard_normal(3 * N)
+    x0, it0, rel0 = a.pcg(b, rtol=1e-10, max_iter=2000)
+    for k in (-300, 300):
+        x1, it1, rel1 = a.pcg(np.ldexp(b, k), rtol=1e-10, max_iter=2000)
+        assert it1 == it0 and rel1 == rel0
+        assert x1.tobytes() == np.ldexp(x0, k).tobytes()
+
+
 def test_solver_needs_an_assembly(gpu):
     m = cube_mesh(5, seed=1, op="ela")
     a = gpu(0)
