@@ -235,7 +235,11 @@ int mfem_wait(mfem_context *ctx, long long ticket);
  * block-Jacobi inverse is the masked, inverted diagonal block that
  * prec_inversion builds, src/Fortran/elasclpr.f:19-27). */
 /* y = A x; x and y are DEVICE pointers (nbNodes*opDim doubles), enqueued on the
- * context stream. */
+ * context stream.  FP64 values: an FP64 FMA chain per row.  FP32 values: every
+ * product exact (x scaled by a power of two and split into two FP32 parts) and
+ * summed in double-float, within a few 2^-48 of the row's sum of |a x|; rows
+ * the split cannot serve (entries below 2^-60 of max |x|, non-finite values)
+ * take the FP64 chain. */
 int mfem_spmv(mfem_context *ctx, const double *x, double *y, int constrained);
 /* z = P r with the block-Jacobi preconditioner; DEVICE pointers. */
 int mfem_prec_apply(mfem_context *ctx, const double *r, double *z);

@@ -11,8 +11,14 @@
 // so the operator is M A M + (I - M) with M the 0/1 mask of free DOFs, whose
 // block-Jacobi inverse is exactly the masked, inverted diagonal block.
 //
+// Arithmetic: with FP64 values the operator is an FP64 FMA chain per row; with
+// FP32 values (the FP32 assembly) it runs on the FP32 pipes in double-float
+// (x scaled by a power of two and split into FP32 hi + lo, exact hi products,
+// TwoSum accumulation), GB300's FP64 pipe being 1/64 of its FP32 rate.
+//
 // Reductions are deterministic: fixed grid, fixed tree order in each CTA, CTA
-// partials summed by one CTA in index order.
+// partials summed in index order by the CTA that finishes last (inside CG) or
+// by one CTA.
 #include <algorithm>
 #include <cmath>
 
