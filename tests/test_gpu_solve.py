@@ -184,6 +184,23 @@ def test_pcg_scale_equivariant(gpu, precision):
         assert x1.tobytes() == np.ldexp(x0, k).tobytes()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_pcg_stops_at_the_iteration_limit(gpu, precision):
+    """maxIter below what the tolerance needs: exactly maxIter iterations (also
+    when maxIter is not a multiple of the iterations enqueued per look at the
+    stop flag: the flag freezes the iterate), and the same bits when repeated."""
+    m, a, row, col, vals, prec, markf = _assembled(gpu, "ela", n=9, precision=precision)
+    N = len(row) - 1
+    b = np.random.default_rng(13).standard_normal(3 * N)
+    x5, it5, rel5 = a.pcg(b, rtol=1e-14, max_iter=5)
+    assert it5 == 5 and rel5 > 1e-14
+    x13, it13, rel13 = a.pcg(b, rtol=1e-14, max_iter=13)   # not a multiple of the batch
+    assert it13 == 13 and np.isfinite(rel13)
+    # a repeated limited solve gives the same iterate
+    x5b, it5b, rel5b = a.pcg(b, rtol=1e-14, max_iter=5)
+    assert it5b == 5 and rel5b == rel5 and x5b.tobytes() == x5.tobytes()
+
+
 def test_solver_needs_an_assembly(gpu):
     m = cube_mesh(5, seed=1, op="ela")
     a = gpu(0)
