@@ -266,8 +266,8 @@ int mfem_pcg(mfem_context *ctx, const double *b, double *x, double rtol, int max
  * Its scratch is one fixed array inside the library of at most 131072 elements
  * (16 MiB of gradient records), held by every GPU that loads the library until
  * the process exits; larger meshes get MFEM_ERR_CAPACITY.  The first call on a
- * device looks the array's device address up (and may load the module holding
- * it), so make that first call before any stream capture.  Work is enqueued on
+ * device looks the array's device address up (a runtime query that may load
+ * the module holding it and synchronise).  Work is enqueued on
  * `stream` (a cudaStream_t, NULL for the legacy default stream) without waiting.
  * All calls share the one array and every call overwrites it: calls that overlap
  * on the GPU (e.g. on two streams) race and must be serialised by the caller.
