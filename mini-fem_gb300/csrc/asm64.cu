@@ -245,8 +245,8 @@ k_edge_units64(const int2 *__restrict__ unitPos, int nUnits, const int *__restri
     for (int a = 0; a < 3; a++)
 #pragma unroll
         for (int bb = 0; bb < 3; bb++) {
-            v[3 * a + bb] = acc[3 * a + bb];
-            w[3 * bb + a] = acc[3 * a + bb];
+            __stcs(v + 3 * a + bb, acc[3 * a + bb]);   // written once: evict first
+            __stcs(w + 3 * bb + a, acc[3 * a + bb]);
         }
     }
 }

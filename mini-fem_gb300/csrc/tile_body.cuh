@@ -134,47 +134,50 @@ __device__ __forceinline__ void ela_accumulate2(Kahan *acc, float4 gj0, float4 g
 
 // One 3x3 FP32 block to base[9p .. 9p+8] with three or four 16-, 8- and
 // 4-byte stores chosen by the block's address modulo 16, instead of nine 4-byte
-// stores: fewer memory transactions per block.
+// stores: fewer memory transactions per block.  The stores are streaming
+// (st.global.cs, evict first): the values are written once, and the L2 keeps
+// the coordinates and weights that neighbouring tiles gather again (0.608 ->
+// 0.592 ms at 100^3).
 __device__ __forceinline__ void store_block9(float *base, size_t p, const float v[9]) {
     float *o = base + p * 9;
     const unsigned mis = (unsigned)(reinterpret_cast<uintptr_t>(o) >> 2) & 3u;
     if (mis == 0u) {
-        *reinterpret_cast<float4 *>(o) = make_float4(v[0], v[1], v[2], v[3]);
-        *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4], v[5], v[6], v[7]);
-        o[8] = v[8];
+        __stcs(reinterpret_cast<float4 *>(o), make_float4(v[0], v[1], v[2], v[3]));
+        __stcs(reinterpret_cast<float4 *>(o + 4), make_float4(v[4], v[5], v[6], v[7]));
+        __stcs(o + 8, v[8]);
     } else if (mis == 1u) {
-        o[0] = v[0];
-        *reinterpret_cast<float2 *>(o + 1) = make_float2(v[1], v[2]);
-        *reinterpret_cast<float4 *>(o + 3) = make_float4(v[3], v[4], v[5], v[6]);
-        *reinterpret_cast<float2 *>(o + 7) = make_float2(v[7], v[8]);
+        __stcs(o + 0, v[0]);
+        __stcs(reinterpret_cast<float2 *>(o + 1), make_float2(v[1], v[2]));
+        __stcs(reinterpret_cast<float4 *>(o + 3), make_float4(v[3], v[4], v[5], v[6]));
+        __stcs(reinterpret_cast<float2 *>(o + 7), make_float2(v[7], v[8]));
     } else if (mis == 2u) {
-        *reinterpret_cast<float2 *>(o) = make_float2(v[0], v[1]);
-        *reinterpret_cast<float4 *>(o + 2) = make_float4(v[2], v[3], v[4], v[5]);
-        *reinterpret_cast<float2 *>(o + 6) = make_float2(v[6], v[7]);
-        o[8] = v[8];
+        __stcs(reinterpret_cast<float2 *>(o), make_float2(v[0], v[1]));
+        __stcs(reinterpret_cast<float4 *>(o + 2), make_float4(v[2], v[3], v[4], v[5]));
+        __stcs(reinterpret_cast<float2 *>(o + 6), make_float2(v[6], v[7]));
+        __stcs(o + 8, v[8]);
     } else {
-        o[0] = v[0];
-        *reinterpret_cast<float4 *>(o + 1) = make_float4(v[1], v[2], v[3], v[4]);
-        *reinterpret_cast<float4 *>(o + 5) = make_float4(v[5], v[6], v[7], v[8]);
+        __stcs(o + 0, v[0]);
+        __stcs(reinterpret_cast<float4 *>(o + 1), make_float4(v[1], v[2], v[3], v[4]));
+        __stcs(reinterpret_cast<float4 *>(o + 5), make_float4(v[5], v[6], v[7], v[8]));
     }
 }
 
 // The same for a 3x3 FP64 block (72 bytes, 8-byte aligned): four 16-byte
-// stores and one 8-byte store.
+// stores and one 8-byte store, streaming.
 __device__ __forceinline__ void store_block9(double *base, size_t p, const double v[9]) {
     double *o = base + p * 9;
     if (reinterpret_cast<uintptr_t>(o) & 15u) {
-        o[0] = v[0];
-        *reinterpret_cast<double2 *>(o + 1) = make_double2(v[1], v[2]);
-        *reinterpret_cast<double2 *>(o + 3) = make_double2(v[3], v[4]);
-        *reinterpret_cast<double2 *>(o + 5) = make_double2(v[5], v[6]);
-        *reinterpret_cast<double2 *>(o + 7) = make_double2(v[7], v[8]);
+        __stcs(o + 0, v[0]);
+        __stcs(reinterpret_cast<double2 *>(o + 1), make_double2(v[1], v[2]));
+        __stcs(reinterpret_cast<double2 *>(o + 3), make_double2(v[3], v[4]));
+        __stcs(reinterpret_cast<double2 *>(o + 5), make_double2(v[5], v[6]));
+        __stcs(reinterpret_cast<double2 *>(o + 7), make_double2(v[7], v[8]));
     } else {
-        *reinterpret_cast<double2 *>(o) = make_double2(v[0], v[1]);
-        *reinterpret_cast<double2 *>(o + 2) = make_double2(v[2], v[3]);
-        *reinterpret_cast<double2 *>(o + 4) = make_double2(v[4], v[5]);
-        *reinterpret_cast<double2 *>(o + 6) = make_double2(v[6], v[7]);
-        o[8] = v[8];
+        __stcs(reinterpret_cast<double2 *>(o), make_double2(v[0], v[1]));
+        __stcs(reinterpret_cast<double2 *>(o + 2), make_double2(v[2], v[3]));
+        __stcs(reinterpret_cast<double2 *>(o + 4), make_double2(v[4], v[5]));
+        __stcs(reinterpret_cast<double2 *>(o + 6), make_double2(v[6], v[7]));
+        __stcs(o + 8, v[8]);
     }
 }
 
