@@ -417,7 +417,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 }
                 quad_combine(acc);
                 if (writer) {
-                    if (p >= 0) values[p] = acc.value();
+                    if (p >= 0) __stcs(values + p, acc.value());
                     if (PREC) {
                         sRes[kResStride * rl] = acc.s;
                         sRes[kResStride * rl + 1] = acc.c;
@@ -467,7 +467,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                 const int r = sDiag[rl].x;
                 const float *res = sRes + kResStride * rl;
                 if (OP == MFEM_OP_LAP) {
-                    precOut[r] = rcp64(f32_to_f64(res[0]) - f32_to_f64(res[1]));
+                    __stcs(precOut + r, rcp64(f32_to_f64(res[0]) - f32_to_f64(res[1])));
                 } else {
                     double d[6];
 #pragma unroll
@@ -517,8 +517,8 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
                     if (q == b) { acc.s = x; acc.c = 0.f; } else acc.add(x);
                 }
                 const float v = acc.value();
-                values[ent.x] = v;
-                if (ent.y >= 0) values[ent.y] = v;
+                __stcs(values + ent.x, v);   // written once: evict first, as store_block9
+                if (ent.y >= 0) __stcs(values + ent.y, v);
             } else {
                 Kahan acc[9];
                 // two contributions per pass, summed as one term (their
