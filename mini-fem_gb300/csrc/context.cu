@@ -378,6 +378,12 @@ int mfem_create(mfem_context **out, int device) {
 int mfem_destroy(mfem_context *ctx) {
     if (!ctx) return MFEM_ERR_INVALID_ARG;
     cudaSetDevice(ctx->c.device);
+    if (ctx->c.side) {
+        cudaStreamSynchronize(ctx->c.side);
+        cudaStreamDestroy(ctx->c.side);
+    }
+    if (ctx->c.sideFork) cudaEventDestroy(ctx->c.sideFork);
+    if (ctx->c.sideJoin) cudaEventDestroy(ctx->c.sideJoin);
     if (ctx->c.stream) {
         cudaStreamSynchronize(ctx->c.stream);
         cudaStreamDestroy(ctx->c.stream);

@@ -112,6 +112,11 @@ struct Context {
     int device = 0;
     KernelTimer timer;
     cudaStream_t stream = nullptr;
+    // second stream for independent kernels of one step (the FP64 gather's
+    // diagonal and off-diagonal units), forked from and joined to `stream`
+    // by the two events; made on first use, destroyed with the context
+    cudaStream_t side = nullptr;
+    cudaEvent_t sideFork = nullptr, sideJoin = nullptr;
     std::string lastError;
 
     // mesh
