@@ -37,9 +37,17 @@ void gather_fp64_sets(const Context &c, int op, const double *coef, double *rec,
 
 }  // namespace mfem
 
+// FP64 batch: meshes are spread over this many concurrent branches of the
+// graph (each with its own gradient-record buffer), so that small meshes that
+// cannot fill the GPU alone run side by side
+constexpr int kBatchBranches = 4;
+
 struct mfem_batch {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side[kBatchBranches - 1] = {};   // the other branches while capturing
+    cudaEvent_t fork = nullptr, join[kBatchBranches - 1] = {};
+    size_t maxRec = 0;                            // doubles of one branch's record buffer
     std::string lastError;
     struct Item {
         mfem_context *ctx;
@@ -61,6 +69,11 @@ struct mfem_batch {
             for (auto &h : g)
                 if (h) cudaGraphExecDestroy(h);
         for (Item *it : items) delete it;
+        for (auto &x : side)
+            if (x) cudaStreamDestroy(x);
+        if (fork) cudaEventDestroy(fork);
+        for (auto &e : join)
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -148,7 +161,8 @@ void prepare(mfem_batch &b) {
     MFEM_CUDA(cudaMemcpy(b.order.ptr, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
     b.hilo.reserve(sizeof(float4) * 2 * b.totalNodes);
     b.prec.reserve(sizeof(double) * b.totalPrec);
-    b.recs.reserve(sizeof(double) * maxRec);
+    b.maxRec = maxRec;
+    b.recs.reserve(sizeof(double) * maxRec * kBatchBranches);
     b.counters.reserve(sizeof(int) * 8);
     // mesh table
     std::vector<BatchMesh> tab(b.items.size());
@@ -219,12 +233,26 @@ void record32(mfem_batch &b, bool withPrec) {
     check_launch("k_batch_tile32");
 }
 
+// The FP64 batch as kBatchBranches concurrent branches forked from and joined
+// to b.stream: each mesh (all its coefficient sets, which share its gradient
+// records) goes to the branch with the least work so far (elements x sets),
+// with that branch's record buffer.  The meshes write disjoint outputs; the
+// singular-block counter is an integer sum.
 void record64(mfem_batch &b, bool withPrec) {
     int *cnt = b.counters.as<int>();
     MFEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * 8, b.stream));
+    MFEM_CUDA(cudaEventRecord(b.fork, b.stream));
+    for (auto &x : b.side) MFEM_CUDA(cudaStreamWaitEvent(x, b.fork, 0));
+    long long load[kBatchBranches] = {};
     for (auto *it : b.items) {
         Context &c = it->ctx->c;
         const int dim = op_dim(it->op);
+        int k = 0;
+        for (int j = 1; j < kBatchBranches; j++)
+            if (load[j] < load[k]) k = j;
+        load[k] += (long long)c.nbElem * it->nSets;
+        cudaStream_t st = k == 0 ? b.stream : b.side[k - 1];
+        double *rec = b.recs.as<double>() + (size_t)k * b.maxRec;
         for (int s = 0; s < it->nSets; s++) {
             const double *coef = it->hasCoef
                 ? it->coef.as<double>() + (size_t)s * c.nbElem * (it->op == MFEM_OP_LAP ? 1 : 2)
@@ -232,9 +260,13 @@ void record64(mfem_batch &b, bool withPrec) {
             double *vals = b.values64.as<double>() + it->valOff + (size_t)s * c.nnz * dim;
             double *prec = withPrec ? b.prec.as<double>() + it->precOff + (size_t)s * c.nbNodes * dim
                                     : nullptr;
-            gather_fp64_sets(c, it->op, coef, b.recs.as<double>(), vals, prec,
-                             c.hasMask ? c.mask.as<unsigned char>() : nullptr, cnt, b.stream, s > 0);
+            gather_fp64_sets(c, it->op, coef, rec, vals, prec,
+                             c.hasMask ? c.mask.as<unsigned char>() : nullptr, cnt, st, s > 0);
         }
+    }
+    for (int j = 0; j < kBatchBranches - 1; j++) {
+        MFEM_CUDA(cudaEventRecord(b.join[j], b.side[j]));
+        MFEM_CUDA(cudaStreamWaitEvent(b.stream, b.join[j], 0));
     }
 }
 
@@ -289,6 +321,9 @@ int mfem_batch_create(mfem_batch **out, int device) {
     b->device = device;
     const int rc = mfem::guarded(b, [](mfem_batch &bb) {
         MFEM_CUDA(cudaStreamCreateWithFlags(&bb.stream, cudaStreamNonBlocking));
+        for (auto &x : bb.side) MFEM_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+        MFEM_CUDA(cudaEventCreateWithFlags(&bb.fork, cudaEventDisableTiming));
+        for (auto &e : bb.join) MFEM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     });
     if (rc != MFEM_OK) {
         delete b;
