@@ -211,13 +211,23 @@ void prepare(mfem_batch &b) {
 }
 
 void record32(mfem_batch &b, bool withPrec) {
+    // the per-mesh coordinate splits and weights (two small launches a mesh)
+    // over the concurrent branches, joined before the persistent kernel
     float4 *hi = b.hilo.as<float4>();
-    for (auto *it : b.items) {
+    MFEM_CUDA(cudaEventRecord(b.fork, b.stream));
+    for (auto &x : b.side) MFEM_CUDA(cudaStreamWaitEvent(x, b.fork, 0));
+    for (size_t m = 0; m < b.items.size(); m++) {
+        auto *it = b.items[m];
         Context &c = it->ctx->c;
-        split_coords(c, hi + 2 * it->nodeOff, b.stream);
+        const int k = (int)(m % kBatchBranches);
+        cudaStream_t st = k == 0 ? b.stream : b.side[k - 1];
+        split_coords(c, hi + 2 * it->nodeOff, st);
         const long long n = (long long)c.nbElem * (it->hasCoef ? it->nSets : 1);
-        weights32_all(it->op, it->hasCoef ? it->coef.as<double>() : nullptr, n, it->w32.as<float2>(),
-                      b.stream);
+        weights32_all(it->op, it->hasCoef ? it->coef.as<double>() : nullptr, n, it->w32.as<float2>(), st);
+    }
+    for (int j = 0; j < kBatchBranches - 1; j++) {
+        MFEM_CUDA(cudaEventRecord(b.join[j], b.side[j]));
+        MFEM_CUDA(cudaStreamWaitEvent(b.stream, b.join[j], 0));
     }
     int *cnt = b.counters.as<int>();
     MFEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * 8, b.stream));
