@@ -125,6 +125,28 @@ def test_gather_fp64_bit_exact_vs_oracle(gpu, n, op, seed, coef, jit, order):
     assert prec.tobytes() == ref["prec"].tobytes()
 
 
+@pytest.mark.parametrize("op", ["lap", "ela"])
+def test_fp64_gather_same_bits_concurrent_and_serial(gpu, op):
+    """The diagonal and off-diagonal unit kernels run concurrently on two
+    streams; with per-kernel profiling on they run one after the other.  Both
+    give the oracle's bits (values and preconditioner)."""
+    m = cube_mesh(12, seed=21, op=op)
+    a = gpu(0)
+    a.set_mesh(m.coord, m.elemToNode)
+    a.create_nodeToNode("reference")
+    a.set_coefficients(op, m.coef)
+    a.set_check_bounds(O.checkbounds(m.boundNodesCode))
+    a.assembly(op, "fp64", "gather", prec=True)
+    v1, p1 = a.values(), a.prec()
+    a.profile(True)
+    a.assembly(op, "fp64", "gather", prec=True)
+    v2, p2 = a.values(), a.prec()
+    a.profile(False)
+    assert v1.tobytes() == v2.tobytes() and p1.tobytes() == p2.tobytes()
+    ref = O.full(m, op=op, coef=m.coef)
+    assert v1.tobytes() == ref["values"].tobytes() and p1.tobytes() == ref["prec"].tobytes()
+
+
 def test_elem_to_edge_matches_reference(gpu):
     m = cube_mesh(8, seed=3)
     a = gpu(0)
