@@ -60,7 +60,11 @@ int mfem_destroy(mfem_context *ctx);
 const char *mfem_last_error(const mfem_context *ctx);
 const char *mfem_status_string(int status);
 int mfem_abi_version(void);
-/* The CUDA stream every call of this context is ordered on (cudaStream_t). */
+/* The CUDA stream every call of this context is ordered on (cudaStream_t).  A
+ * call may fan independent kernels out to a second stream of the context (the
+ * FP64 gather's diagonal and off-diagonal units), always joined back to this
+ * stream before the call returns: work enqueued on it afterwards, or a wait on
+ * it, sees the call complete. */
 int mfem_get_stream(mfem_context *ctx, void **stream);
 
 /* ---- mesh (src/IO.cc:61-96 arrays) ----------------------------------------- */
