@@ -48,6 +48,17 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
         : "memory");
 }
 
+// A node's split coordinates (hi float4, lo float4: one 32-byte sector, 32-byte
+// aligned, read-only in this kernel) by one 256-bit load.
+__device__ __forceinline__ void ld_node_hl(const float4 *p, float4 &h, float4 &l) {
+    double a, b, c, d;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(a), "=d"(b), "=d"(c), "=d"(d) : "l"(p));
+    h = make_float4(__int_as_float(__double2loint(a)), __int_as_float(__double2hiint(a)),
+                    __int_as_float(__double2loint(b)), __int_as_float(__double2hiint(b)));
+    l = make_float4(__int_as_float(__double2loint(c)), __int_as_float(__double2hiint(c)),
+                    __int_as_float(__double2loint(d)), __int_as_float(__double2hiint(d)));
+}
+
 // 8-byte asynchronous global -> shared copy (both addresses 8-byte aligned)
 __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -306,8 +317,10 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     float4 *Xl = Xh + T.nNodes;
     for (int i = tid; i < T.nNodes; i += kTileThreads) {
         const int n = P.nodes[T.nodeBegin + i];
-        Xh[i] = M.hl[2 * n];
-        Xl[i] = M.hl[2 * n + 1];
+        float4 h, l;
+        ld_node_hl(M.hl + 2 * n, h, l);
+        Xh[i] = h;
+        Xl[i] = l;
     }
     cp_async_wait_all();
     __syncthreads();
