@@ -275,7 +275,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
     float *sRes = reinterpret_cast<float *>(sm + L.res);              // kResStride floats per row
     unsigned short *sC = reinterpret_cast<unsigned short *>(sm + L.contrib);
     int4 *sOff = reinterpret_cast<int4 *>(sm + L.off);
-    int2 *sDiag = reinterpret_cast<int2 *>(sm + L.diag);
+    int4 *sDiag = reinterpret_cast<int4 *>(sm + L.diag);
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + L.bar);           // two barriers
     const int tid = threadIdx.x, lane = tid & 31;
     __shared__ int sNext;      // next off-diagonal unit of phase 2
@@ -290,7 +290,7 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         // make the initialised barriers visible to the TMA (async) proxy
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const unsigned bc = (unsigned)T.nContribPad * 2u, bd = (unsigned)T.nRowsPad * 8u;
+        const unsigned bc = (unsigned)T.nContribPad * 2u, bd = (unsigned)T.nRowsPad * 16u;
         mbar_expect_tx(bar, bc + bd + ctl.extraTx);
         if (bc) bulk_g2s(sC, P.contrib + T.contribBegin, bc, bar);
         if (bd) bulk_g2s(sDiag, P.diagEnt + T.diagBegin, bd, bar);
@@ -416,10 +416,10 @@ __device__ __forceinline__ bool tile_body(const TileDesc &T, const TileMesh &M, 
         for (int base = 0; base < T.nRows; base += diagThreads / 4) {
             const int rl = base + (tid >> 2);
             const bool active = rl < T.nRows;
-            const int2 de = active ? sDiag[rl] : make_int2(0, 0);
+            const int4 de = active ? sDiag[rl] : make_int4(0, 0, -1, 0);
             const int b = (unsigned)de.y >> 8, n = de.y & 0xff;
             const bool writer = active && part == 0;
-            const int p = writer ? M.diagPos[de.x] : -1;
+            const int p = writer ? de.z : -1;
             if (OP == MFEM_OP_LAP) {
                 Kahan acc;
                 for (int q = b + part; q < b + n; q += 4) {

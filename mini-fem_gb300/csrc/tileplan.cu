@@ -302,7 +302,7 @@ struct PlanDst {
     int *elems, *nodes;
     ushort4 *lconn;
     int4 *offEnt;
-    int2 *diagEnt;
+    int4 *diagEnt;
     unsigned short *contrib;
     int *counts;                     // counting pass: per tile (elements, nodes, contributions, off entries)
     int *rowTotals;                  // per position: the row's (contributions, off entries), from the counting pass
@@ -437,7 +437,7 @@ k_tile_lists(PlanSrc S, PlanDst D) {
         }
         // padding of the segments (zeros)
         for (int i = T.nContrib + tid; i < T.nContribPad; i += blockDim.x) D.contrib[T.contribBegin + i] = 0;
-        for (int i = T.nRows + tid; i < T.nRowsPad; i += blockDim.x) D.diagEnt[T.diagBegin + i] = make_int2(0, 0);
+        for (int i = T.nRows + tid; i < T.nRowsPad; i += blockDim.x) D.diagEnt[T.diagBegin + i] = make_int4(0, 0, -1, 0);
         __syncthreads();
     }
     // rows: one warp per row, lanes over the row's entries
@@ -483,7 +483,7 @@ k_tile_lists(PlanSrc S, PlanDst D) {
                 const int start = P.rowC[lr] + rowC + sc;
                 const int meta = (start << 8) | cnt;
                 if (cc == r) {
-                    D.diagEnt[T.diagBegin + lr] = make_int2(r, meta);
+                    D.diagEnt[T.diagBegin + lr] = make_int4(r, meta, b + m, 0);   // b + m: the CSR position of (r, r)
                 } else {
                     int tpos = -1;
                     if (pc >= s && pc < s + nR) {   // a row of this tile: the transposed position
@@ -520,7 +520,7 @@ k_tile_lists(PlanSrc S, PlanDst D) {
                 D.rowTotals[2 * (s + lr)] = rowC;
                 D.rowTotals[2 * (s + lr) + 1] = rowO;
             } else if (!hasDiag) {
-                D.diagEnt[D.desc[t].diagBegin + lr] = make_int2(r, 0);
+                D.diagEnt[D.desc[t].diagBegin + lr] = make_int4(r, 0, -1, 0);
             }
         }
     }
@@ -714,7 +714,7 @@ void build_tile_plan_device(Context &c) {
     D.lconn = (ushort4 *)alloc(tp.lconn, (size_t)nE * sizeof(ushort4));
     D.nodes = (int *)alloc(tp.nodes, (size_t)nN * 4);
     D.offEnt = (int4 *)alloc(tp.offEnt, (size_t)nO * sizeof(int4));
-    D.diagEnt = (int2 *)alloc(tp.diagEnt, (size_t)nD * sizeof(int2));
+    D.diagEnt = (int4 *)alloc(tp.diagEnt, (size_t)nD * sizeof(int4));
     D.contrib = (unsigned short *)alloc(tp.contrib, (size_t)nC * 2);
     MFEM_CUDA(cudaMemsetAsync(status, 0, sizeof(int), st));
     k_tile_lists<true><<<nTiles, kPlanThreads, smem, st>>>(S, D);

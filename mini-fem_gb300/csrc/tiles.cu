@@ -69,7 +69,7 @@ k_tile32(TilePlanView P, TileMesh M, TileSets S, SmemLayout L, float qthr2, int 
         if (ctl.pfDist > 0 && nt < ctl.nTiles) {
             const TileDesc N = P.desc[nt];
             prefetch_range(P.contrib, (size_t)N.contribBegin * 2, (size_t)N.nContribPad * 2);
-            prefetch_range(P.diagEnt, (size_t)N.diagBegin * 8, (size_t)N.nRowsPad * 8);
+            prefetch_range(P.diagEnt, (size_t)N.diagBegin * 16, (size_t)N.nRowsPad * 16);
             prefetch_range(P.offEnt, (size_t)N.offBegin * 16, (size_t)N.nOffPad * 16);
             prefetch_range(P.lconn, (size_t)N.elemBegin * 8, (size_t)N.nElem * 8);
             prefetch_range(P.elems, (size_t)N.elemBegin * 4, (size_t)N.nElem * 4);
@@ -132,7 +132,7 @@ SmemLayout smem_layout(int maxElem, int maxContribPad, int maxOffPad, int maxRow
     L.w = maxElem * 64;                                 // gradients: 4 float4 per element
     L.contrib = L.w + round_up(maxElem * 8, 16);        // weights: float2 per element
     L.diag = L.contrib + round_up(maxContribPad * 2, 16);
-    L.off = L.diag + maxRowsPad * 8;                    // after phase 1: off-diagonal table,
+    L.off = L.diag + maxRowsPad * 16;                   // after phase 1: off-diagonal table,
     L.res = L.off + maxOffPad * 16;                     //   then the row results
     L.x = L.off;                                        // during phase 1: coordinates,
     L.q = L.x + maxNodes * 32;                          //   then the flagged-element queue
@@ -167,7 +167,7 @@ TilePlanView plan_view(const TilePlan &tp) {
     P.lconn = tp.lconn.as<ushort4>();
     P.nodes = tp.nodes.as<int>();
     P.offEnt = tp.offEnt.as<int4>();
-    P.diagEnt = tp.diagEnt.as<int2>();
+    P.diagEnt = tp.diagEnt.as<int4>();
     P.contrib = tp.contrib.as<unsigned short>();
     return P;
 }

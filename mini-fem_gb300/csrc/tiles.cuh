@@ -16,7 +16,7 @@ constexpr int kResStride = 13;
 // contribution lists they reference.  Segment starts are 16-byte aligned and the
 // *Pad counts cover whole 16-byte units, so each segment is one bulk copy.
 struct TileDesc {
-    int diagBegin, nRows, nRowsPad;          // into diagEnt: (row, meta)
+    int diagBegin, nRows, nRowsPad;          // into diagEnt: (row, meta, CSR position of (row, row) or -1, 0)
     int elemBegin, nElem;                    // into elems
     int offBegin, nOff, nOffPad;             // into offEnt: (pos, transposed pos or -1, meta, 0)
     int contribBegin, nContrib, nContribPad; // into contrib (u16: local elem << 4 | slot j << 2 | slot k)
@@ -32,7 +32,7 @@ struct TilePlanView {
     const ushort4 *lconn;        // their nodes as indices into the tile's node list
     const int *nodes;            // each tile's nodes (0-based ids, ascending)
     const int4 *offEnt;
-    const int2 *diagEnt;
+    const int4 *diagEnt;
     const unsigned short *contrib;
 };
 
