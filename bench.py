@@ -144,7 +144,7 @@ def kernel_bytes(name, E, N, nnz, n_edge_units, fp32):
 # dram__bytes_read.sum + dram__bytes_write.sum divided by its 1,232,274 tets);
 # traffic grows in proportion to the mesh, so the full launch's traffic is this
 # times E.
-TRAFFIC_PER_ELEM = {"tile32+prec": (145.177344e6 + 94.161152e6) / 1232274,
+TRAFFIC_PER_ELEM = {"tile32+prec": (145.482752e6 + 94.085376e6) / 1232274,
                     "edge_units64": (282.084864e6 + 198.790656e6) / 1232274}
 
 # FP64-pipe thread instructions per element of each FP64 gather kernel (ela with
