@@ -818,7 +818,7 @@ def run_solve(args):
                      "spmv_hbm_frac": round(byts / (ms * 1e-3) / 1e9 / hbm, 4),
                      "spmv_bytes": byts,
                      "spmv_arithmetic": "FP64 FMA chain, 9 per block" if prec == "fp64" else
-                     "FP32 double-float (exact hi products, sums within a few 2^-48 of sum|a x|), "
+                     "FP32 double-float (exact hi products, sums within 15 x 2^-48 of sum|a x|), "
                      "x split into hi/lo FP32 by one extra pass inside the timed call",
                      "pcg_iterations": it, "pcg_relres": rel, "pcg_s": round(wall, 4),
                      "pcg_ms_per_iteration": round(wall * 1e3 / max(it, 1), 4)}

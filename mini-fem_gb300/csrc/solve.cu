@@ -25,6 +25,7 @@
 #include "context.h"
 #include "dmul_int.cuh"
 #include "elem32.cuh"
+#include "spmv_df.cuh"
 
 namespace mfem {
 
@@ -291,8 +292,8 @@ constexpr int kSpmvBlocksPerLane = 2;
 
 // y = A x for FP32 values from the split xs: the hi products by TwoSum into s,
 // every error term and lo product into t; the four lanes' (s, t) merged in
-// double-float; y = (s + t) 2^kx.  A lane's s + t is within a few 2^-48 of
-// sum |a x| of its blocks.
+// double-float, each lane's pair renormalized after every chunk; y = (s + t)
+// 2^kx, within 15 x 2^-48 of sum |a x| over the row (spmv_df.cuh).
 //
 // Four lanes share a block row and take its blocks in chunks of 8 (lane l the
 // blocks l and l + 4): a chunk's values go to shared memory by 16-byte
@@ -376,18 +377,12 @@ k_spmv32(const int *__restrict__ rowPtr, const int *__restrict__ col, const floa
             for (int i = 0; i < D; i++) {
 #pragma unroll
                 for (int jj = 0; jj < D; jj++) {
-                    const float a = v[D * i + jj];
-                    const float p = a * xv[j][jj].x;
-                    const float e = fmaf(a, xv[j][jj].x, -p);
-                    const float s1 = s[i] + p;
-                    const float bp = s1 - s[i];
-                    const float err = (s[i] - (s1 - bp)) + (p - bp);
-                    s[i] = s1;
-                    t[i] = fmaf(a, xv[j][jj].y, t[i]) + (e + err);
-                    pmax = fmaxf(pmax, fabsf(p));
+                    pmax = fmaxf(pmax, spdf::accumulate(s[i], t[i], v[D * i + jj], xv[j][jj].x, xv[j][jj].y));
                 }
             }
         }
+#pragma unroll
+        for (int i = 0; i < D; i++) spdf::renormalize(s[i], t[i]);
         __syncwarp(gmask);
     }
     // the row's four lanes: largest product, finiteness and the double-float
@@ -400,11 +395,7 @@ k_spmv32(const int *__restrict__ rowPtr, const int *__restrict__ col, const floa
         for (int d = 0; d < D; d++) {
             const float s2 = __shfl_xor_sync(0xffffffffu, s[d], off);
             const float t2 = __shfl_xor_sync(0xffffffffu, t[d], off);
-            const float s1 = s[d] + s2;
-            const float bp = s1 - s[d];
-            const float err = (s[d] - (s1 - bp)) + (s2 - bp);
-            s[d] = s1;
-            t[d] = (t[d] + t2) + err;
+            spdf::merge(s[d], t[d], s2, t2);
         }
     }
 #pragma unroll
