@@ -1,6 +1,7 @@
 """Full-size case of the benchmark (100^3 nodes, 5,821,794 tets): bit-exact FP64
-gather against the oracle on the whole matrix, and size-independent properties
-(symmetry, zero row sums of the Laplacian, idempotent re-assembly)."""
+gather against the oracle on the whole matrix, size-independent properties
+(symmetry, zero row sums of the Laplacian, idempotent re-assembly), and the
+operator on the result (sampled rows of y = A x exactly, CG residuals)."""
 import numpy as np
 import pytest
 
@@ -83,3 +84,45 @@ def test_fullsize_fp32_within_tolerance_and_batch_equal(gpu, mesh):
     assert b.values(0, 0, "fp32").tobytes() == v32.tobytes()
     assert b.prec(0, 0).tobytes() == p32.tobytes()
     b.close()
+
+
+def test_fullsize_spmv_sampled_rows_and_pcg(gpu, mesh):
+    """The operator at full size, for the FP64 and the FP32 assembly: 4,000
+    sampled rows of y = A x against the correctly rounded product (the bounds
+    of spmv_exact, relative to each row's sum of |a x|), and block-Jacobi CG on
+    the Dirichlet-constrained system to 1e-8, its residual recomputed on the
+    host from the assembled values."""
+    import scipy.sparse as sp
+    import torch
+    from spmv_exact import BOUND, exact_apply
+    a = gpu(0)
+    a.set_mesh(mesh.coord, mesh.elemToNode)
+    row, col = a.create_nodeToNode("sorted")
+    a.set_coefficients("ela", mesh.coef)
+    markf = O.checkbounds(mesh.boundNodesCode)
+    a.set_check_bounds(markf)
+    N = len(row) - 1
+    f = (np.asarray(markf).reshape(3, N).T == 0).reshape(-1).astype(np.float64)   # 1: free DOF
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(3 * N)
+    rows = np.sort(rng.choice(N, 4000, replace=False))
+    idx = np.concatenate([np.arange(row[r], row[r + 1]) for r in rows])
+    srow = np.concatenate([[0], np.cumsum(row[rows + 1] - row[rows])])
+    for precision in ("fp64", "fp32"):
+        a.assembly("ela", precision, "gather", prec=True)
+        vals = a.values_f32().astype(np.float64) if precision == "fp32" else a.values()
+        xd = torch.from_numpy(x).cuda()
+        yd = torch.empty_like(xd)
+        torch.cuda.synchronize()
+        a.spmv(xd.data_ptr(), yd.data_ptr(), False)
+        a.synchronize()
+        torch.cuda.synchronize()
+        y = yd.cpu().numpy().reshape(N, 3)[rows].reshape(-1)
+        ref, scale = exact_apply(srow, col[idx], vals.reshape(-1, 9)[idx].reshape(-1), 3, x)
+        assert np.max(np.abs(y - ref) / scale) < BOUND[precision], precision
+        b = rng.standard_normal(3 * N)
+        xs, it, rel = a.pcg(b, rtol=1e-8, max_iter=3000)
+        assert rel <= 1e-8 and 0 < it < 3000, (precision, it, rel)
+        A = sp.bsr_matrix((vals.reshape(-1, 3, 3), col - 1, row), shape=(3 * N, 3 * N))
+        r = b - (f * (A @ (f * xs)) + (1 - f) * xs)
+        assert np.linalg.norm(r) <= 2e-8 * np.linalg.norm(b), precision
