@@ -533,7 +533,9 @@ __global__ void k_cg_start(CgScalars *sc, const double *sums, double tol2, int m
     sc->stop = (sc->rr <= tol2 * sc->bb || maxIter <= 0) ? 1 : 0;
 }
 
-// x += alpha p; r -= alpha q; z = P r; partials of r . z and r . r.
+// x += alpha p; r -= alpha q; z = P r; partials of r . z and r . r.  Grid-
+// stride over the nodes (nCta == gridDim.x CTAs, a few nodes per thread), so
+// that the CTA reductions and the last CTA's sum are spread over more work.
 template <int D>
 __global__ void __launch_bounds__(kThreads)
 k_cg_update(const double *__restrict__ prec, CgScalars *__restrict__ sc,
@@ -541,10 +543,9 @@ k_cg_update(const double *__restrict__ prec, CgScalars *__restrict__ sc,
             double *__restrict__ r, double *__restrict__ z, int N, double *__restrict__ partial,
             int nCta, CgLink link) {
     if (sc->stop) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double alpha = sc->alpha;
     double rz = 0.0, rr = 0.0;
-    if (i < N) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         double rv[D];
 #pragma unroll
         for (int d = 0; d < D; d++) {
@@ -739,11 +740,12 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     // the tolerance returns at once, so the iterate stays the converged one
     const int *stop = &sc->stop;
     const unsigned gDir = (unsigned)std::min<long long>(blocks_for((long long)n, kThreads), kMaxCtas);
+    const int gUpd = (int)std::min<long long>(nCtaNodes, kMaxCtas);
     while (!hostSc->stop) {
         for (int k = 0; k < kCgBatch; k++) {
             spmv(c, vp, vq, mask, partial, stop, ps, link);     // q = A p; p . q; alpha
-            if (D == 3) k_cg_update<3><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes, link);
-            else k_cg_update<1><<<nCtaNodes, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, nCtaNodes, link);
+            if (D == 3) k_cg_update<3><<<gUpd, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, gUpd, link);
+            else k_cg_update<1><<<gUpd, kThreads, 0, s>>>(P, sc, vp, vq, vx, vr, vz, c.nbNodes, partial, gUpd, link);
             if (D == 3) k_cg_direction<3><<<gDir, kThreads, 0, s>>>(sc, vz, vp, ps.xs, mask, (long long)n, link);
             else k_cg_direction<1><<<gDir, kThreads, 0, s>>>(sc, vz, vp, ps.xs, mask, (long long)n, link);
         }
