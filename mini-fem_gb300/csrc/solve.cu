@@ -534,8 +534,9 @@ __global__ void k_cg_start(CgScalars *sc, const double *sums, double tol2, int m
 }
 
 // x += alpha p; r -= alpha q; z = P r; partials of r . z and r . r.  Grid-
-// stride over the nodes (nCta == gridDim.x CTAs, a few nodes per thread), so
-// that the CTA reductions and the last CTA's sum are spread over more work.
+// stride over the nodes (nCta == gridDim.x CTAs, four per SM: several nodes
+// per thread), so that the CTA reductions and the last CTA's sum are spread
+// over more work.
 template <int D>
 __global__ void __launch_bounds__(kThreads)
 k_cg_update(const double *__restrict__ prec, CgScalars *__restrict__ sc,
@@ -740,7 +741,11 @@ void pcg(Context &c, const double *b, double *x, double rtol, int maxIter, int c
     // the tolerance returns at once, so the iterate stays the converged one
     const int *stop = &sc->stop;
     const unsigned gDir = (unsigned)std::min<long long>(blocks_for((long long)n, kThreads), kMaxCtas);
-    const int gUpd = (int)std::min<long long>(nCtaNodes, kMaxCtas);
+    // the vector update: four CTAs per SM (measured at 100^3 against 2, 3, 8
+    // per SM and 1,024 or 2,048 CTAs)
+    int sms = 0;
+    MFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+    const int gUpd = std::max(1, std::min(nCtaNodes, 4 * sms));
     while (!hostSc->stop) {
         for (int k = 0; k < kCgBatch; k++) {
             spmv(c, vp, vq, mask, partial, stop, ps, link);     // q = A p; p . q; alpha
